@@ -1,0 +1,1 @@
+/* libtiff is only used for input I/O; the oracle reads raw or Analyze. */
