@@ -1,0 +1,397 @@
+"""Throughput benchmark: WaP outer iterations per second at 256^3 x 192 projections.
+
+Workload (the 256^3 GPU-vs-CPU configuration): a 256^3 FP32 foam phantom
+(band-limited noise thresholded at the 70th percentile), compressed over time
+(u_z = -0.25 t (z - z0) plus a smooth RBF perturbation of <= 6 voxels), 192
+cone-beam projections at 384x384 on golden-ratio angles, one deformation state
+each, Poisson noise at I0 = 1e4.  Seeded synthetic data stands in for the
+reference's (unpublished) scans.  48 frames (4 projections each, windows +-3),
+schedule of PSART::Render: 5 CP iterations x 2 SART sweeps, a 4-level L1-TV
+flow (tol 0.008, lambda 0.05, <= 3000 iterations, 3 warps) for every
+adjacent pair, then warp-and-project over every frame's window.
+
+A "step" is one frame's complete share of an outer iteration (its CP + SART
+steps, the flow of the pair it starts, its warp-and-project window): an
+outer iteration is exactly F such steps, so value = outer-iter/s =
+1 / (F * mean step time).  A whole outer iteration at this size is minutes of
+GPU time, which is why the unit streamed here is the frame share.
+
+value times the steps on the device with inputs resident; e2e times the same
+steps with each step's inputs (its projection window) copied host->device
+from pinned memory and its results (volume and flow) copied back.
+
+--impl reference times the reference algorithm on the host CPU (the oracle
+port of the reference's OpenMP code) on a bounded sample: one forward and
+back projection, one warp, one CP frame pass and a few primal-dual iterations
+at full size per step, composed into outer-iter/s from the exact op counts of
+the GPU run's schedule.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(REPO, "warp-and-project-tomography_gb300")
+for _p in (PKG, os.path.join(REPO, "tests"), os.path.join(REPO, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "WaP outer-iter/s at 256^3 x 192 proj"
+PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
+# Compulsory bytes of one primal-dual iteration per voxel: read and write the
+# 10 dual components (y1..y3, y4) and the 3 flow components, read the
+# 4-component linearisation (ux, uy, uz, ut); tau and sigma2 derive from u.
+PD_BYTES_PER_VOXEL = 4 * (10 + 10 + 3 + 3 + 4)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--det", type=int, default=384)
+    ap.add_argument("--nproj", type=int, default=192)
+    ap.add_argument("--scales", type=int, default=4)
+    ap.add_argument("--flow-iters", type=int, default=3000)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def workload(args, torch, ctx_factory):
+    """Phantom, deformation, projections; returns (ctx, projs_device, angles, meta)."""
+    import phantoms as P
+    n, d, nproj = args.n, args.det, args.nproj
+    nframes = nproj // 4
+    torch.manual_seed(2)
+    base = torch.from_numpy(P.foam(n, seed=0)).cuda()
+    rbf = torch.from_numpy(P.rbf_flow(n, amp=6.0, sigma=12.0, seed=1)).cuda()
+    ang = P.golden_angles(nproj)
+    ctx = ctx_factory(n, d, nproj, nframes, ang)
+    z = torch.arange(n, device="cuda", dtype=torch.float32).view(n, 1, 1).expand(n, n, n)
+    projs = torch.empty((nproj, d, d), device="cuda")
+    img = torch.empty((d, d), device="cuda")
+    # backward-mapped deformation, trilinear (grid_sample) -- data generation only
+    zz, yy, xx = torch.meshgrid(*(torch.arange(n, device="cuda", dtype=torch.float32),) * 3, indexing="ij")
+    for k in range(nproj):
+        t = k / float(nproj - 1)
+        ux = t * rbf[0]
+        uy = t * rbf[1]
+        uz = -0.25 * t * (z - n / 2) + t * rbf[2]
+        g = torch.stack([(xx - ux) / (n - 1) * 2 - 1, (yy - uy) / (n - 1) * 2 - 1, (zz - uz) / (n - 1) * 2 - 1], -1)
+        vol_t = torch.nn.functional.grid_sample(base.view(1, 1, n, n, n), g.view(1, n, n, n, 3), align_corners=True,
+                                                mode="bilinear", padding_mode="zeros").view(n, n, n).contiguous()
+        ctx.forward(k, vol_t, img)
+        ctx.synchronize()
+        projs[k].copy_(img)
+    kappa = 3.0 / float(projs.max())
+    I0 = 1e4
+    counts = torch.poisson(I0 * torch.exp(-kappa * projs), generator=None)
+    projs = (-torch.log(torch.clamp(counts, min=1.0) / I0) / kappa).contiguous()
+    del base, rbf, z, zz, yy, xx
+    torch.cuda.empty_cache()
+    return ctx, projs, ang, dict(nframes=nframes)
+
+
+class ClockSampler:
+    FIELDS = "clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 6:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[2:6]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_sample(args, counts, threads):
+    """Time the oracle port of the reference's CPU path on a bounded sample and
+    compose seconds per outer iteration from the GPU run's op counts."""
+    import oracle as O
+    import phantoms as P
+    orc = O.Oracle()
+    n, d = args.n, args.det
+    scan = O.make_scan((n, n, n), (d, d), args.nproj, nframes_cli=args.nproj // 4, threads=threads)
+    scan.gmax = 1.0
+    vol = P.foam(n, seed=0)
+    ang = P.golden_angles(args.nproj)
+    t = {}
+    t0 = time.time()
+    img, ln, wt = orc.forward(scan, ang[5], vol)
+    t["fp"] = time.time() - t0
+    corr = np.ascontiguousarray(img * 1e-3, np.float32)
+    v2 = vol.copy()
+    t0 = time.time()
+    orc.bp_voxel(scan, ang[5], corr, [8, n - 8, 8, n - 8, 8, n - 8], 0, v2)
+    t["bp"] = time.time() - t0
+    flow = P.rbf_flow(n, amp=3.0, seed=1)
+    aabb = [0, n, 0, n, 0, n]
+    t0 = time.time()
+    orc.advect([n] * 3, aabb, flow, vol, 0.5, threads)
+    t["advect"] = time.time() - t0
+    nv = n ** 3
+    ytv = np.zeros((3, n, n, n), np.float32)
+    ytp = np.zeros((n, n, n), np.float32)
+    xp = np.zeros((n, n, n), np.float32)
+    box = np.array([8, n - 8] * 3, np.int32)
+    t0 = time.time()
+    orc.lib.orc_cp_dual(O.ctypes.byref(scan), box, vol, vol, ytv, ytp)
+    orc.lib.orc_cp_primal(O.ctypes.byref(scan), box, 1, ytp.ctypes.data, ytp, ytv, v2, xp)
+    orc.lib.orc_cp_overrelax(np.array([n] * 3, np.int32), box, v2, xp, ytp)
+    t["cp"] = time.time() - t0
+    V = np.zeros((3, n, n, n), np.float32)
+    Y = [np.zeros((3, n, n, n), np.float32) for _ in range(3)] + [np.zeros((n, n, n), np.float32)]
+    roi = [8] * 6
+    t0 = time.time()
+    orc.flow_level([n] * 3, vol, v2, V, *Y, 0.0, 0.05, 0, 1, aabb, roi, deterministic=0)
+    t1 = time.time()
+    orc.flow_level([n] * 3, vol, v2, V, *Y, 0.0, 0.05, 3, 1, aabb, roi, deterministic=0)
+    t2 = time.time()
+    t["pd_voxel_iter"] = max((t2 - t1) - (t1 - t0), 1e-9) / 3.0 / nv
+    sec = (counts["projections"] * t["fp"] + counts["backprojections"] * t["bp"] +
+           counts["advect_voxels"] / nv * t["advect"] + counts["cp_frame_passes"] * t["cp"] +
+           counts["pd_voxel_iters"] * t["pd_voxel_iter"])
+    sample = ("composed from one 256^3->384^2 forward projection, one bicubic backprojection, one warp, one CP "
+              "frame pass and 1 vs 4 primal-dual iterations at 256^3, weighted by the op counts of one outer "
+              "iteration")
+    return sec, t, sample
+
+
+def run_gb300(args):
+    import torch
+    import wap
+    import build
+    rank, world, local, dist = dist_init(args)
+    torch.cuda.set_device(local)
+    build.build()
+    stream = torch.cuda.Stream()
+
+    def factory(n, d, nproj, nframes, ang):
+        c = wap.Context(wap.make_scan((n, n, n), (d, d), nproj, nframes_cli=nframes), ang, device=local)
+        c.set_stream(stream.cuda_stream)
+        return c
+
+    with torch.cuda.stream(stream):
+        ctx, projs, ang, meta = workload(args, torch, factory)
+    F = meta["nframes"]
+    ctx.set_projections_device(projs)
+    ctx.level_setup(0)
+    sched = wap.reference_schedule(n_cp=5, nb_sart=2, wp_frames=F, flow_iters=args.flow_iters,
+                                   flow_scales=args.scales, flow_tol=0.008, cut=8, bp_exact=1)
+    # Initial reconstruction (untimed): one CP + SART pass over all frames so the
+    # flow solver sees structured volumes, as it does after the first pass.
+    init = wap.reference_schedule(n_cp=1, nb_sart=1, wp_frames=0, flow_iters=0, flow_scales=1, cut=8, bp_exact=0)
+    init.flow_warps = 0
+    ctx.outer_iteration(init)
+    ctx.set_profiling(True)
+    n, d = args.n, args.det
+    nv = n ** 3
+    np_ = d * d
+    # pinned host mirrors for the end-to-end leg
+    h_projs = torch.empty((args.nproj, d, d), pin_memory=True)
+    h_projs.copy_(projs)
+    h_vol = torch.empty((n, n, n), pin_memory=True)
+    h_flow = torch.empty((3, n, n, n), pin_memory=True)
+    nf, st, en, ft, tu = wap.level_frames(ctx.scan, 0)
+
+    # results of a step go back to pinned host memory (end-to-end leg)
+    def d2h(f):
+        ctx.call("wap_frame_volume_download", f, h_vol.data_ptr())
+        ctx.call("wap_frame_flow_download", f, h_flow.data_ptr())
+
+    frames = list(range(F - 1))
+    order = [frames[(rank * 7 + i) % len(frames)] for i in range(args.warmup + args.steps)]
+    for i in range(args.warmup):
+        f = order[i]
+        with torch.cuda.stream(stream):
+            projs[int(st[f]):int(en[f]) + 1].copy_(h_projs[int(st[f]):int(en[f]) + 1], non_blocking=True)
+        ctx.outer_iteration_frames(sched, f, f + 1)
+        d2h(f)
+    stream.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_dev, t_e2e = 0.0, 0.0
+    agg = dict(pd_voxel_iters=0.0, advect_voxels=0.0, projections=0, backprojections=0, cp_frame_passes=0,
+               kernel_launches=0, flow_pd_iterations=0, ms_pd=0.0, pd_timed=0, ms_cp=0.0, ms_flow=0.0, ms_wap=0.0)
+    h2d_bytes = 0
+    pd_vox = 0
+    for i in range(args.warmup, args.warmup + args.steps):
+        f = order[i]
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        s0, s1 = int(st[f]), int(en[f]) + 1
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            projs[s0:s1].copy_(h_projs[s0:s1], non_blocking=True)
+            ev[1].record(stream)
+        s = ctx.outer_iteration_frames(sched, f, f + 1)
+        with torch.cuda.stream(stream):
+            ev[2].record(stream)
+            d2h(f)
+            ev[3].record(stream)
+        stream.synchronize()
+        t_dev += ev[1].elapsed_time(ev[2]) / 1e3
+        t_e2e += ev[0].elapsed_time(ev[3]) / 1e3
+        h2d_bytes += (s1 - s0) * np_ * 4
+        for k in agg:
+            agg[k] += getattr(s, k)
+        pd_vox = max(pd_vox, s.pd_timed_voxels)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        import torch.distributed as tdist
+        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        t_dev, t_e2e = float(tt[0]), float(tt[1])
+        tdist.barrier()
+    K = args.steps
+    value = world * (K / F) / t_dev
+    e2e = world * (K / F) / t_e2e
+    pd_ms = agg["ms_pd"] / max(agg["pd_timed"], 1)
+    achieved = PD_BYTES_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    result = {
+        "metric": METRIC, "value": value, "unit": "outer-iter/s", "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": t_dev / K * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded foam phantom, RBF+compression, Poisson I0=1e4)",
+        "config": {"workload": "256^3 volume, 192 proj at 384^2, 48 frames, 5 CP x 2 SART, 4-level L1-TV flow "
+                               "(tol 0.008, <=3000 its, 3 warps), WaP over all windows; step = one frame's share "
+                               "of an outer iteration",
+                   "volume": [n, n, n], "detector": [d, d], "projections": args.nproj, "frames": F,
+                   "parallelism": "replicas" if world > 1 else "single", "l2": "working set > L2 (GBs per step)",
+                   "bp_arithmetic": "reference double (exact)"},
+        "e2e": {"value": e2e, "unit": "outer-iter/s", "h2d_bytes_per_step": h2d_bytes // K,
+                "d2h_bytes_per_step": 4 * nv * 4},
+        "gpu_launches": int(agg["kernel_launches"]),
+        "roofline": {"kernel": "flow primal-dual iteration (pd_primal + pd_dual) at 256^3", "bound": "hbm",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "bytes_per_voxel": PD_BYTES_PER_VOXEL,
+                     "ms_per_launch": pd_ms},
+        "phase_ms_per_step": {"cp_sart": agg["ms_cp"] / K, "flow": agg["ms_flow"] / K, "wap": agg["ms_wap"] / K},
+        "pd_iterations_per_step": agg["flow_pd_iterations"] / K,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        counts = {k: agg[k] * F / K for k in ("projections", "backprojections", "advect_voxels", "cp_frame_passes",
+                                               "pd_voxel_iters")}
+        threads = os.cpu_count() or 1
+        sec, parts, sample = cpu_sample(args, counts, threads)
+        result["cpu_baseline"] = {"value": 1.0 / sec, "unit": "outer-iter/s", "cores": threads, "kind": "port",
+                                  "sample": sample, "component_seconds": parts}
+    if rank == 0:
+        print(json.dumps(result))
+    if dist:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    # Op counts of one outer iteration of the same schedule at 256^3 x 192
+    # (48 frames, windows of <= 7, 5 CP x 2 SART, 3 warps, 4 levels).
+    import oracle as O
+    orc = O.Oracle()
+    F = args.nproj // 4
+    nf, st, en, ft, tu = orc.level_frames(F, args.nproj, 0)
+    win = (en - st + 1).astype(np.int64)
+    n = args.n
+    nv = n ** 3
+    lvl = sum((1.0 / 8 ** l) for l in range(args.scales))
+    counts = {"projections": int(5 * 2 * win.sum() + win.sum()), "backprojections": int(5 * 2 * win.sum() + win.sum()),
+              "advect_voxels": float(2 * win.sum() * nv + (F - 1) * 3 * lvl * nv),
+              "cp_frame_passes": 5 * F, "pd_voxel_iters": float((F - 1) * 3 * (args.flow_iters + 1) * lvl * nv)}
+    threads = os.cpu_count() or 1
+    times = []
+    for i in range(args.warmup + args.steps):
+        sec, parts, sample = cpu_sample(args, counts, threads)
+        if i >= args.warmup:
+            times.append(sec)
+    sec = float(np.mean(times))
+    v = 1.0 / sec
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "outer-iter/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "256^3 volume, 192 proj at 384^2, 48 frames (composed CPU sample)"},
+        "cpu_baseline": {"value": v, "unit": "outer-iter/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "outer-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }))
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)

@@ -1,0 +1,232 @@
+/* wap.h -- C ABI of the GB300-native warp-and-project (WaP) reconstruction
+ * hot path.
+ *
+ * The reference (WaP19) exposes its hot path as C++ entry points, not as an
+ * FFI; each function below replaces one of them, named in its comment with
+ * the reference file:line it stands in for.  Arguments are plain pointers and
+ * sizes.  Array layouts follow the reference's CImg images: idx = x + W*(y +
+ * H*z), channels planar (a 3-component flow is three consecutive volumes).
+ *
+ * Pointer kinds: arguments named h_* are host memory, d_* are device memory
+ * on the context's device.  Every call returns WAP_OK or a WAP_E* status and
+ * never throws; wap_last_error() gives the message of the last failure on that
+ * context.  A context is used by one host thread at a time; work is ordered on
+ * the context's stream (wap_set_stream), and calls that return host data
+ * synchronise that stream.
+ */
+#ifndef WAP_WAP_H
+#define WAP_WAP_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WAP_API __attribute__((visibility("default")))
+
+enum {
+  WAP_OK = 0,
+  WAP_EINVAL = 1,   /* bad argument or size */
+  WAP_ENOMEM = 2,   /* device allocation failed */
+  WAP_ECUDA = 3,    /* CUDA runtime error */
+  WAP_ESTATE = 4,   /* call out of order (e.g. no level set up) */
+  WAP_ENODEV = 5    /* no usable GPU */
+};
+
+typedef struct wap_ctx wap_ctx;
+
+/* Scan geometry and solver weights: the reference's command-line options
+ * (main.cpp:15-138) plus the projection count it hard-codes (main.cpp:198). */
+typedef struct {
+  int vol[3];       /* -f  volume dims */
+  int det[2];       /* -u  detector W, H */
+  int nproj;        /* projections in the stack (main.cpp:198) */
+  int nframes_cli;  /* -v  frames at time level 0 */
+  double vs;        /* -c  voxel spacing */
+  double ds;        /* -d  detector spacing */
+  double sid;       /* -g  source to iso-centre distance */
+  double sdd;       /* -j  source to detector distance */
+  double oxyz[3];   /* --oxyz  volume centre offset */
+  double alpha;     /* -a  SART relaxation */
+  double tv_w;      /* -s  spatial TV weight */
+  double tp_w;      /* -t  temporal weight */
+} wap_scan_desc;
+
+/* One outer iteration's schedule (WaP_Tomo.cpp:478-492, 711-727). */
+typedef struct {
+  int n_cp;          /* Chambolle-Pock iterations (nb_volOpt[level]) */
+  int nb_sart;       /* SART sweeps per proximal call (nb_proxiSART) */
+  int nb_projwarp;   /* warp-and-project passes (nb_projwarp) */
+  int wp_frames;     /* frames the WaP pass visits (WaP_Tomo.cpp:801) */
+  float flow_tol;    /* 0.008 */
+  float flow_lambda; /* 0.05 */
+  int flow_iters;    /* 3000 */
+  int flow_warps;    /* 3 */
+  float flow_eta;    /* 0.5 */
+  float flow_sigma;  /* 0.8 */
+  int flow_scales;   /* 5 */
+  int cut;           /* ROI margin, 8 */
+  int bp_exact;      /* 1: bicubic BP in the reference's double arithmetic; 0: FP32 FMA */
+} wap_schedule;
+
+/* Counters of the last outer iteration (reset by each wap_outer_iteration*). */
+typedef struct {
+  long long flow_pd_iterations;  /* primal-dual iterations over all pairs, levels, warps */
+  long long fp_launches;
+  long long kernel_launches;     /* every kernel this library launched */
+  double ms_cp, ms_flow, ms_wap; /* device time per phase (CUDA events) */
+  double pd_voxel_iters;         /* sum over PD iterations of the level's voxel count */
+  double advect_voxels;          /* voxels warped (all advect calls) */
+  long long projections;         /* forward projections (one per frame job) */
+  long long backprojections;     /* voxel-driven backprojections */
+  long long cp_frame_passes;     /* CP dual + primal + over-relaxation, per frame */
+  double ms_pd;                  /* profiled: device time of the PD iterations at the largest grid */
+  long long pd_timed;            /* profiled: PD iterations in ms_pd */
+  long long pd_timed_voxels;     /* profiled: voxels of that grid */
+} wap_stats;
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Builds VolumeData + PSART state for a scan (main.cpp:195-219,
+ * WaP_Tomo.cpp:228-434): per-projection geometry (PSART::RotateVolume +
+ * Scene/_calculateMatrix, WaP_Tomo.cpp:1764-1797) is computed once here.
+ * h_angles_deg: nproj angles in degrees (WaP_Tomo.cpp:324-331). */
+WAP_API int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_deg, int device);
+WAP_API void wap_destroy(wap_ctx *ctx);
+WAP_API const char *wap_last_error(const wap_ctx *ctx);
+WAP_API int wap_set_stream(wap_ctx *ctx, void *cuda_stream);
+WAP_API int wap_synchronize(wap_ctx *ctx);
+WAP_API int wap_get_stats(wap_ctx *ctx, wap_stats *out);
+/* 1: time every primal-dual iteration of the flow solver with CUDA events on
+ * the context's stream (wap_stats.ms_pd); 0 (default): no per-launch events. */
+WAP_API int wap_set_profiling(wap_ctx *ctx, int on);
+
+/* Projection stack W*H*nproj (PSART ctor loading + get_split, WaP_Tomo.cpp:339);
+ * also sets G_Max = max of the first projection image, projslevel[0][0]
+ * (WaP_Tomo.cpp:347-348). */
+WAP_API int wap_upload_projections(wap_ctx *ctx, const float *h_projs);
+WAP_API int wap_set_projections_device(wap_ctx *ctx, const float *d_projs);
+WAP_API float wap_gmax(const wap_ctx *ctx);
+WAP_API int wap_set_gmax(wap_ctx *ctx, float gmax);
+
+/* Frame windows of a time level (VolumeData::ReadStructuredFile,
+ * VolumeData.cpp:118-228).  Returns the frame count, fills up to cap entries. */
+WAP_API int wap_level_frames(const wap_scan_desc *scan, int level, int *start, int *end, float *ftime, float *tunit,
+                             int cap);
+
+/* Device state of one time level: F volumes, F flows, CP state (zeroed).
+ * Frames and flows are then read/written with the calls below. */
+WAP_API int wap_level_setup(wap_ctx *ctx, int level);
+WAP_API int wap_level_nframes(const wap_ctx *ctx);
+WAP_API int wap_frame_volume_upload(wap_ctx *ctx, int frame, const float *h_vol);
+WAP_API int wap_frame_volume_download(wap_ctx *ctx, int frame, float *h_vol);
+WAP_API int wap_frame_flow_upload(wap_ctx *ctx, int frame, const float *h_flow);
+WAP_API int wap_frame_flow_download(wap_ctx *ctx, int frame, float *h_flow);
+WAP_API float *wap_frame_volume_device(wap_ctx *ctx, int frame);
+WAP_API float *wap_frame_flow_device(wap_ctx *ctx, int frame);
+/* Next time level: frame 2i and 2i+1 take frame i (WaP_Tomo.cpp:834-849). */
+WAP_API int wap_level_advance(wap_ctx *ctx);
+
+/* ---- projector (device pointers) ---------------------------------------- */
+
+/* GenerateImage_GetCorrections (TypicalRayProducer.core.h:230-268) with
+ * SingleScalarVolumePrepare/RayCasterPrepare (SingleScalarVolume.core.h:366,
+ * RayCaster.core.h:191): projection d_img, ray length d_len and sample count
+ * d_weight (W*H each; any may be NULL) of d_vol at projection `proj`. */
+WAP_API int wap_forward_project(wap_ctx *ctx, int proj, const float *d_vol, float *d_img, float *d_len,
+                                float *d_weight);
+
+/* Batched form: njobs volumes, each at its own projection. */
+WAP_API int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const float *const *h_d_vols,
+                                      float *const *h_d_imgs, float *const *h_d_lens, float *const *h_d_weights);
+
+/* PSART correction + dual update (WaP_Tomo.cpp:1530-1555): c = (p - Ax - y)/
+ * (len + 1), y += alpha c.  d_dual may be NULL (y = 0, WaP_Tomo.cpp:1261-1284). */
+WAP_API int wap_correction(wap_ctx *ctx, int n, const float *d_meas, const float *d_img, const float *d_len,
+                           float *d_dual, float *d_corr);
+
+/* Voxel-driven bicubic backprojection (WaP_Tomo.cpp:1557-1628 mode 0: vol +=
+ * alpha*g then clamp [0,G_Max] over the box; WaP_Tomo.cpp:1294-1374 mode 1:
+ * d_vol += g).  box = x0,x1,y0,y1,z0,z1 half-open; exact selects the
+ * reference's double arithmetic. */
+WAP_API int wap_backproject_voxel(wap_ctx *ctx, int proj, const float *d_corr, const int *box, int mode, int exact,
+                                  float *d_vol);
+
+/* Ray-driven matched backprojection: the reference's back-projection mode of
+ * the ray caster (SingleScalarVolume.core.h:85-96,149-199), FP32 atomics.
+ * d_contrib / d_weight are accumulated into (zero them first). */
+WAP_API int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_contrib, float *d_weight);
+
+/* ---- warp (device pointers) --------------------------------------------- */
+
+/* advection::advect (advection.h:117-146): d_out (nc channels) = d_src warped
+ * by the 3-channel d_vel over time dt inside the box aabb. */
+WAP_API int wap_advect(wap_ctx *ctx, const int *dims, const float *aabb, const float *d_vel, const float *d_src,
+                       int nc, float dt, float *d_out);
+
+/* ---- optical flow (device pointers) ------------------------------------- */
+
+/* CImg get_blur(sigma) (Deriche, CImg.h:33276-33285), get_resize(..,5)
+ * (CImg.h:28432-28610) and get_gradient("xyz",0) (CImg.h:34570-34590) as the
+ * flow pyramid uses them. */
+WAP_API int wap_blur(wap_ctx *ctx, const int *dims, int nc, float sigma, const float *d_src, float *d_out);
+WAP_API int wap_resize(wap_ctx *ctx, const int *dims, int nc, const float *d_src, const int *odims, float *d_out);
+
+/* optical_flow::L1TVOpticalFlowNonlinear3D (optical_flow.h:88-995): one
+ * pyramid level.  d_V (3 ch), d_Y1..d_Y3 (3 ch), d_Y4 (1 ch) are updated in
+ * place (ROI written, as the reference does).  roi6 = margins.  Returns the
+ * primal-dual iteration count of each warp in h_iters (nwarps ints). */
+WAP_API int wap_flow_level(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, float *d_V,
+                           float *d_Y1, float *d_Y2, float *d_Y3, float *d_Y4, float tol, float lambda,
+                           int max_iters, int nwarps, const float *aabb, const int *roi6, int *h_iters);
+
+/* optical_flow::L1TVOpticalFlowNonlinear_MultiScale3D (optical_flow.h:1002-1126)
+ * as PSART::Render calls it (WaP_Tomo.cpp:711-753): Y start at zero, d_V0 is
+ * the warm start, d_Vout the finest flow.  Returns total PD iterations via
+ * h_total_iters (may be NULL). */
+WAP_API int wap_flow_multiscale(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2,
+                                const float *d_V0, float tol, float lambda, int max_iters, int nwarps, float eta,
+                                float sigma, int scales, const int *cut6, float *d_Vout, long long *h_total_iters);
+
+/* ---- solver (context state) -------------------------------------------- */
+
+/* PSART::SART_Proximal_Operator (WaP_Tomo.cpp:1424-1678) on one frame of the
+ * current level; use_cut selects the ROI box of Render (cut margins). */
+WAP_API int wap_sart_prox(wap_ctx *ctx, int frame, int nb_sart, int cut, int exact);
+
+/* PSART::WarpAndProjct (WaP_Tomo.cpp:1207-1421) for one projection. */
+WAP_API int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exact);
+
+/* One outer iteration of PSART::Render at the current level
+ * (WaP_Tomo.cpp:514-827): CP prior + SART over all frames, flow for every
+ * adjacent pair, warp-and-project over the schedule's frames. */
+WAP_API int wap_outer_iteration(wap_ctx *ctx, const wap_schedule *sched, wap_stats *stats);
+
+/* The same outer iteration restricted to frames [f0, f1): their CP + SART
+ * steps, the flows of the pairs (f, f+1) they start, and their WaP windows.
+ * [0, F) is wap_outer_iteration; a single frame is one frame's share of the
+ * iteration's work (the unit the throughput benchmark streams). */
+WAP_API int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sched, int f0, int f1, wap_stats *stats);
+
+/* Per-projection matrices as the projector kernels use them (host only, no
+ * GPU needed): the reference's PixelsToModel, ModelToVolume, model-view x
+ * VolumeToModel, and EyePos (TypicalRayProducer.cpp:157-232,
+ * TypicalRayProducer.core.h:255-258). */
+WAP_API int wap_projection_geometry(const wap_scan_desc *scan, double angle_deg, float *h_p2m, float *h_m2v,
+                                    float *h_mvv2m, float *h_eye);
+
+/* ---- CG (device pointers) ---------------------------------------------- */
+
+/* image_cg::cg (cg.h:11-55) on A = a*I - b*Laplacian (Neumann): x updated in
+ * place.  mode 0 is textbook CG; mode 1 reproduces the reference's update
+ * (image_blas::add reassigns p before reading it, image_blas.h:135-149, so
+ * p = r).  Dot products and norms in FP64.  Returns iterations in h_iters. */
+WAP_API int wap_cg_screened_laplacian(wap_ctx *ctx, const int *dims, float a, float b, const float *d_rhs,
+                                      float *d_x, float rel_tol, int max_iters, float abs_tol, int mode,
+                                      int *h_iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WAP_WAP_H */

@@ -1,0 +1,261 @@
+"""GPU parity: every kernel of the C ABI against the CPU oracle on seeded inputs.
+
+Integer/index results (sample counts, traversal) and every path whose
+arithmetic is the reference's are compared bit for bit; the FP32-FMA variants
+and the atomic splat are compared within the stated tolerances.
+"""
+import numpy as np
+import pytest
+
+import phantoms as P
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+N, W, H, NP = 32, 48, 48, 16
+
+
+@pytest.fixture(scope="module")
+def setup(wapmod, orc, torch_cuda):
+    import oracle as O
+    torch = torch_cuda
+    vol = P.ellipsoids(N, seed=0)
+    flow = P.rbf_flow(N, amp=2.0, seed=1)
+    ang = P.golden_angles(NP)
+    oscan = O.make_scan((N, N, N), (W, H), NP, nframes_cli=2)
+    projs = np.stack([orc.forward(oscan, a, vol)[0] for a in ang]).astype(np.float32)
+    projs += np.random.default_rng(2).normal(scale=0.01 * projs.max(), size=projs.shape).astype(np.float32)
+    wscan = wapmod.make_scan((N, N, N), (W, H), NP, nframes_cli=2)
+    ctx = wapmod.Context(wscan, ang)
+    ctx.upload_projections(projs)
+    oscan.gmax = ctx.gmax
+    yield dict(torch=torch, ctx=ctx, vol=vol, flow=flow, ang=ang, oscan=oscan, projs=projs, O=O)
+    ctx.close()
+
+
+def dev(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+def test_gmax_is_max_of_first_projection(setup):
+    assert setup["ctx"].gmax == np.float32(setup["projs"][0].max())
+
+
+def test_forward_projection_bitexact(setup, orc):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    dvol = dev(torch, s["vol"])
+    for p in range(NP):
+        img = torch.zeros((H, W), device="cuda")
+        ln = torch.zeros_like(img)
+        wt = torch.zeros_like(img)
+        ctx.forward(p, dvol, img, ln, wt)
+        ctx.synchronize()
+        oi, ol, ow = orc.forward(s["oscan"], s["ang"][p], s["vol"])
+        assert np.array_equal(host(wt), ow), "sample counts differ at projection %d" % p
+        assert np.array_equal(host(ln), ol)
+        assert np.array_equal(host(img), oi)
+
+
+def test_forward_projection_config0_size(wapmod, orc, torch_cuda):
+    import oracle as O
+    torch = torch_cuda
+    n, d = 64, 96
+    vol = P.ellipsoids(n, seed=4)
+    ang = P.golden_angles(8)
+    ctx = wapmod.Context(wapmod.make_scan((n, n, n), (d, d), 8), ang)
+    oscan = O.make_scan((n, n, n), (d, d), 8)
+    dvol = dev(torch, vol)
+    for p in (0, 3, 7):
+        img = torch.zeros((d, d), device="cuda")
+        wt = torch.zeros_like(img)
+        ctx.forward(p, dvol, img, None, wt)
+        ctx.synchronize()
+        oi, _, ow = orc.forward(oscan, ang[p], vol)
+        assert np.array_equal(host(wt), ow)
+        assert np.array_equal(host(img), oi)
+    ctx.close()
+
+
+def test_correction_and_voxel_backprojection(setup, orc):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    rng = np.random.default_rng(7)
+    p = 5
+    meas = s["projs"][p]
+    img, ln, _ = orc.forward(s["oscan"], s["ang"][p], s["vol"])
+    dual = rng.normal(scale=0.1, size=(H, W)).astype(np.float32)
+    odual = dual.copy()
+    oc = orc.correction(meas, img, ln, odual, s["oscan"].alpha)
+    dd = dev(torch, dual)
+    dc = torch.zeros((H, W), device="cuda")
+    ctx.correction(W * H, dev(torch, meas), dev(torch, img), dev(torch, ln), dd, dc)
+    ctx.synchronize()
+    assert np.array_equal(host(dc), oc)
+    assert np.array_equal(host(dd), odual)
+    box = [8, N - 8, 8, N - 8, 8, N - 8]
+    for mode in (0, 1):
+        base = (s["vol"] * 0.5).astype(np.float32) if mode == 0 else np.zeros_like(s["vol"])
+        ov = orc.bp_voxel(s["oscan"], s["ang"][p], oc, box if mode == 0 else [0, N, 0, N, 0, N], mode, base.copy())
+        for exact in (1, 0):
+            dv = dev(torch, base)
+            ctx.backproject_voxel(p, dc, box if mode == 0 else [0, N, 0, N, 0, N], mode, exact, dv)
+            ctx.synchronize()
+            if exact:
+                assert np.array_equal(host(dv), ov), "exact BP mode %d" % mode
+            else:
+                assert rel_l2(host(dv), ov) < 1e-5, "fast BP mode %d" % mode
+
+
+def test_ray_backprojection_matches_dead_path(setup, orc):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    corr = np.random.default_rng(5).normal(size=(H, W)).astype(np.float32)
+    oc, ow = orc.ray_backproject(s["oscan"], s["ang"][4], corr)
+    dcon = torch.zeros((N, N, N), device="cuda")
+    dw = torch.zeros_like(dcon)
+    ctx.backproject_ray(4, dev(torch, corr), dcon, dw)
+    ctx.synchronize()
+    # FP32 atomics reorder the sums (the reference's own += races under OpenMP).
+    assert rel_l2(host(dcon), oc) < 1e-5
+    assert rel_l2(host(dw), ow) < 1e-5
+
+
+@pytest.mark.parametrize("dt,box", [(0.7, 1), (-1.0, 1), (-1.0, 2)])
+def test_advect_bitexact(setup, orc, dt, box):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    aabb = np.array([0, box * N, 0, box * N, 0, box * N], np.float32)
+    src = np.stack([s["vol"], P.ellipsoids(N, seed=9)])
+    out = torch.zeros((2, N, N, N), device="cuda")
+    ctx.advect([N, N, N], aabb, dev(torch, s["flow"]), dev(torch, src), 2, dt, out)
+    ctx.synchronize()
+    ref = orc.advect([N, N, N], aabb, s["flow"], src.astype(np.float32), dt)
+    assert np.array_equal(host(out), ref)
+
+
+def test_blur_and_resize_bitexact(setup, orc):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    src = s["vol"]
+    out = torch.zeros((N, N, N), device="cuda")
+    ctx.blur([N, N, N], 1, 0.8, dev(torch, src), out)
+    ctx.synchronize()
+    assert np.array_equal(host(out), orc.blur([N, N, N], src, 0.8))
+    for od in [(16, 16, 16), (64, 64, 64), (20, 40, 33), (32, 32, 16)]:
+        o = torch.zeros((3, od[2], od[1], od[0]), device="cuda")
+        ctx.resize([N, N, N], 3, dev(torch, s["flow"]), od, o)
+        ctx.synchronize()
+        assert np.array_equal(host(o), orc.resize([N, N, N], s["flow"], od)), od
+
+
+def _flow_inputs(s, orc):
+    aabb = np.array([0, N, 0, N, 0, N], np.float32)
+    I1 = P.ellipsoids(N, seed=3)
+    I2 = orc.advect([N] * 3, aabb, s["flow"], I1, 1.0)
+    return aabb, I1, I2
+
+
+@pytest.mark.parametrize("tol,iters,nwarps", [(0.0, 120, 2), (0.008, 3000, 1)])
+def test_flow_level_bitexact(setup, orc, tol, iters, nwarps):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    aabb, I1, I2 = _flow_inputs(s, orc)
+    roi = [4] * 6
+    V0 = (s["flow"] * 0.3).astype(np.float32)
+    Y = [np.zeros((3, N, N, N), np.float32) for _ in range(3)] + [np.zeros((N, N, N), np.float32)]
+    oV, oY = V0.copy(), [y.copy() for y in Y]
+    tot, oits = orc.flow_level([N] * 3, I1, I2, oV, *oY, tol, 0.05, iters, nwarps, aabb, roi, deterministic=1)
+    dV = dev(torch, V0)
+    dY = [dev(torch, y) for y in Y]
+    its = ctx.flow_level([N] * 3, dev(torch, I1), dev(torch, I2), dV, *dY, tol, 0.05, iters, nwarps, aabb, roi)
+    assert list(its) == list(oits)
+    assert np.array_equal(host(dV), oV)
+    for a, b in zip(dY, oY):
+        assert np.array_equal(host(a), b)
+
+
+def test_flow_multiscale_bitexact(setup, orc):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    aabb, I1, I2 = _flow_inputs(s, orc)
+    V0 = (s["flow"] * 0.5).astype(np.float32)
+    ov, otot = orc.flow_multiscale([N] * 3, I1, I2, V0, 0.0, 0.05, 60, 2, 0.5, 0.8, 3, [8] * 6)
+    out = torch.zeros((3, N, N, N), device="cuda")
+    tot = ctx.flow_multiscale([N] * 3, dev(torch, I1), dev(torch, I2), dev(torch, V0), 0.0, 0.05, 60, 2, 0.5, 0.8,
+                              3, [8] * 6, out)
+    assert tot == otot
+    assert np.array_equal(host(out), ov)
+
+
+@pytest.mark.parametrize("exact", [1, 0])
+def test_sart_prox(setup, orc, exact):
+    s = setup
+    ctx, O = s["ctx"], s["O"]
+    nf = ctx.level_setup(0)
+    onf, st, en, ft, tu = orc.level_frames(2, NP, 0)
+    assert nf == onf
+    v1 = (s["vol"] * 0.5).astype(np.float32)
+    ctx.upload_volume(1, v1)
+    ctx.sart_prox(1, nb_sart=2, cut=8, exact=exact)
+    got = ctx.download_volume(1)
+    ov, _ = orc.sart_prox(s["oscan"], s["ang"], s["projs"], int(st[1]), int(en[1]), 2, [8, N - 8] * 3, v1.copy())
+    if exact:
+        assert np.array_equal(got, ov)
+    else:
+        assert rel_l2(got, ov) < 1e-4
+
+
+def test_warp_and_project_bitexact(setup, orc):
+    s = setup
+    ctx = s["ctx"]
+    ctx.level_setup(0)
+    _, st, en, ft, tu = orc.level_frames(2, NP, 0)
+    v1 = (s["vol"] * 0.5).astype(np.float32)
+    fl0 = (s["flow"] * 0.7).astype(np.float32)
+    ctx.upload_volume(1, v1)
+    ctx.upload_flow(0, fl0)
+    cur = v1.copy()
+    for ik, rt in [(int(st[1]), -0.6), (int(en[1]), 0.9)]:
+        ctx.warp_and_project(1, ik, rt, exact=1)
+        fwd = fl0 if rt < 0 else np.zeros_like(fl0)
+        cur = orc.warp_and_project(s["oscan"], s["ang"], s["projs"], ik, rt, fwd, fl0, cur.copy())
+        assert np.array_equal(ctx.download_volume(1), cur)
+
+
+def test_outer_iteration_bitexact(setup, orc, wapmod):
+    s = setup
+    ctx, O = s["ctx"], s["O"]
+    F = ctx.level_setup(0)
+    sched_o = O.Schedule(n_cp=2, nb_sart=2, nb_projwarp=1, wp_frames=2, flow_tol=0.0, flow_lambda=0.05,
+                         flow_iters=60, flow_warps=2, flow_eta=0.5, flow_sigma=0.8, flow_scales=2, cut=8,
+                         deterministic=1)
+    sched_w = wapmod.reference_schedule(n_cp=2, nb_sart=2, wp_frames=2, flow_iters=60, flow_scales=2, flow_tol=0.0,
+                                        flow_warps=2)
+    state = dict(vols=np.zeros((F, N, N, N), np.float32), flows=np.zeros((F, 3, N, N, N), np.float32),
+                 ytv=np.zeros((F, 3, N, N, N), np.float32), ytp=np.zeros((F, N, N, N), np.float32),
+                 xbar=np.zeros((F, N, N, N), np.float32), xprev=np.zeros((F, N, N, N), np.float32))
+    for it in range(2):
+        st = ctx.outer_iteration(sched_w)
+        orc.outer_iteration(s["oscan"], sched_o, s["ang"], s["projs"], 0, state)
+        for f in range(F):
+            assert np.array_equal(ctx.download_volume(f), state["vols"][f]), (it, f)
+            assert np.array_equal(ctx.download_flow(f), state["flows"][f]), (it, f)
+        assert st.kernel_launches > 0
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_cg_screened_laplacian(setup, orc, mode):
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    rhs = np.random.default_rng(3).normal(size=(N, N, N)).astype(np.float32)
+    xo = np.zeros_like(rhs)
+    oit = orc.cg_screened_laplacian([N] * 3, 1.0, 0.5, rhs, xo, 1e-5, 200, 1e-9, mode)
+    dx = torch.zeros((N, N, N), device="cuda")
+    it = ctx.cg_screened_laplacian([N] * 3, 1.0, 0.5, dev(torch, rhs), dx, 1e-5, 200, 1e-9, mode)
+    assert abs(it - oit) <= 2
+    assert rel_l2(host(dx), xo) < 1e-4

@@ -1,0 +1,195 @@
+// Semi-Lagrangian warp of a volume by a flow field: advection::advect
+// (advection.h:10-146) with CImg's _cubic_atXYZ (CImg.h:13429-13524).
+//
+// Per voxel: a BFECC-style back-trace p2 = p - dt v(p), p0 = p2 + dt v(p2),
+// q = p2 + (p - p0)/2, then a Catmull-Rom tricubic sample at q limited to the
+// min/max of its 8 trilinear neighbours.  Three clamped-tricubic samples per
+// voxel (two of the 3-channel velocity, one of the source), 72 taps each, all
+// FP32 without contraction so the result matches the reference bit for bit.
+// The world position of each cell centre involves a double division in the
+// reference (cell_grid_to_world); it is tabulated per axis on the host.
+#include <vector>
+
+#include "wap_internal.h"
+
+namespace wap {
+namespace {
+
+struct Grid3 {
+  int n[3];
+  float a0[3], a1[3];  // aabb lower/upper per axis
+};
+
+// CImg's cubic kernel, float (CImg.h:13437-13519).
+__device__ __forceinline__ float cubf(float p, float c, float n, float a, float t) {
+  return c + 0.5f * (t * (-p + n) + t * t * (2 * p - 5 * c + 4 * n - a) + t * t * t * (-p + 3 * c - 3 * n + a));
+}
+
+struct SamplePoint {
+  int ix, iy, iz;    // trilinear cell for the limiter (advection.h:63)
+  int xs[4], ys[4], zs[4];
+  float dx, dy, dz;
+};
+
+// world_to_cell_grid + clamp to [1, n-2] (advection.h:32-36, 54-63) and
+// CImg's tap indices (CImg.h:13431-13439).
+__device__ __forceinline__ SamplePoint locate(const Grid3 &G, float px, float py, float pz) {
+  const float p[3] = {px, py, pz};
+  float g[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    // (float)((double)t - 0.5) is the float subtraction t - 0.5f.
+    const float t = (float)G.n[a] * (p[a] - G.a0[a]) / (G.a1[a] - G.a0[a]);
+    g[a] = t - 0.5f;
+    g[a] = std_max(1.0f, std_min((float)(G.n[a] - 2), g[a]));
+  }
+  SamplePoint s;
+  s.ix = (int)g[0];
+  s.iy = (int)g[1];
+  s.iz = (int)g[2];
+  int *idx[3] = {s.xs, s.ys, s.zs};
+  float *fr[3] = {&s.dx, &s.dy, &s.dz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float hi = (float)(G.n[a] - 1);
+    const float nf = g[a] < 0.0f ? 0.0f : (g[a] > hi ? hi : g[a]);
+    const int x = (int)nf;
+    const float d = nf - (float)x;
+    *fr[a] = d;
+    idx[a][0] = x - 1 < 0 ? 0 : x - 1;
+    idx[a][1] = x;
+    idx[a][2] = d > 0.0f ? x + 1 : x;
+    idx[a][3] = x + 2 >= G.n[a] ? G.n[a] - 1 : x + 2;
+  }
+  return s;
+}
+
+// sample_image (advection.h:49-88) of one channel at a located point.
+__device__ __forceinline__ float sample(const float *__restrict__ img, const Grid3 &G, const SamplePoint &s) {
+  const int nx = G.n[0], nxy = G.n[0] * G.n[1];
+  auto I = [&](int x, int y, int z) { return __ldg(img + (x + nx * y + nxy * z)); };
+  float mn = I(s.ix, s.iy, s.iz), mx = mn;
+  const int o[7][3] = {{1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    const float v = I(s.ix + o[q][0], s.iy + o[q][1], s.iz + o[q][2]);
+    mn = std_min(mn, v);
+    mx = std_max(mx, v);
+  }
+  float planes[4];
+#pragma unroll
+  for (int kz = 0; kz < 4; ++kz) {
+    float rows[4];
+#pragma unroll
+    for (int ky = 0; ky < 4; ++ky) {
+      const int y = s.ys[ky], z = s.zs[kz];
+      rows[ky] = cubf(I(s.xs[0], y, z), I(s.xs[1], y, z), I(s.xs[2], y, z), I(s.xs[3], y, z), s.dx);
+    }
+    planes[kz] = cubf(rows[0], rows[1], rows[2], rows[3], s.dy);
+  }
+  const float c = cubf(planes[0], planes[1], planes[2], planes[3], s.dz);
+  return std_max(mn, std_min(mx, c));
+}
+
+__global__ void __launch_bounds__(128) advect_kernel(Grid3 G, const float *__restrict__ wx,
+                                                     const float *__restrict__ wy, const float *__restrict__ wz,
+                                                     const AdvectJob *__restrict__ jobs, int nc) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int j = blockIdx.y * blockDim.y + threadIdx.y;
+  const int k = blockIdx.z % G.n[2];
+  const AdvectJob job = jobs[blockIdx.z / G.n[2]];
+  if (i >= G.n[0] || j >= G.n[1]) return;
+  const float *__restrict__ vel = job.vel;
+  const float *__restrict__ src = job.src;
+  float *__restrict__ out = job.out;
+  const float tdt = -job.dt;
+  const size_t nv = (size_t)G.n[0] * G.n[1] * G.n[2];
+  const float p[3] = {__ldg(wx + i), __ldg(wy + j), __ldg(wz + k)};
+  // trace (advection.h:101-115) with dt_trace = -dt.
+  SamplePoint s = locate(G, p[0], p[1], p[2]);
+  float v0 = sample(vel, G, s), v1 = sample(vel + nv, G, s), v2 = sample(vel + 2 * nv, G, s);
+  const float p2[3] = {p[0] + tdt * v0, p[1] + tdt * v1, p[2] + tdt * v2};
+  s = locate(G, p2[0], p2[1], p2[2]);
+  v0 = sample(vel, G, s);
+  v1 = sample(vel + nv, G, s);
+  v2 = sample(vel + 2 * nv, G, s);
+  const float p0[3] = {p2[0] - tdt * v0, p2[1] - tdt * v1, p2[2] - tdt * v2};
+  const float q[3] = {p2[0] + (p[0] - p0[0]) * 0.5f, p2[1] + (p[1] - p0[1]) * 0.5f, p2[2] + (p[2] - p0[2]) * 0.5f};
+  s = locate(G, q[0], q[1], q[2]);
+  const size_t o = i + (size_t)G.n[0] * (j + (size_t)G.n[1] * k);
+  for (int c = 0; c < nc; ++c) out[c * nv + o] = sample(src + c * nv, G, s);
+}
+
+// vol += alpha * adv (double, CImg operator* / operator+=), cut(0, G_Max),
+// then max(vol * imROI, 0) with imROI == 1 (WaP_Tomo.cpp:1378-1412).
+__global__ void wap_accumulate_kernel(size_t n, float *__restrict__ vol, const float *__restrict__ adv, double alpha,
+                                      float gmax) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float x = (float)((double)vol[i] + (double)adv[i] * alpha);
+  x = (x < 0.0f) ? 0.0f : ((x > gmax) ? gmax : x);
+  vol[i] = mac_max(x * 1.0f, 0.0f);
+}
+
+__global__ void wap_accumulate_batch_kernel(const AccJob *__restrict__ jobs, size_t n, double alpha, float gmax) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const AccJob jb = jobs[blockIdx.y];
+  float x = (float)((double)jb.vol[i] + (double)jb.adv[i] * alpha);
+  x = (x < 0.0f) ? 0.0f : ((x > gmax) ? gmax : x);
+  jb.vol[i] = mac_max(x * 1.0f, 0.0f);
+}
+
+__global__ void roi_floor_kernel(size_t n, float *__restrict__ vol) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  vol[i] = mac_max(vol[i] * 1.0f, 0.0f);
+}
+
+}  // namespace
+
+void world_table(const int dims[3], const float aabb[6], float *h) {
+  int off = 0;
+  for (int a = 0; a < 3; ++a) {
+    for (int i = 0; i < dims[a]; ++i) {
+      const float gf = (float)i;
+      h[off + i] = (float)(aabb[2 * a] + (gf + 0.5) * (aabb[2 * a + 1] - aabb[2 * a]) / (float)dims[a]);
+    }
+    off += dims[a];
+  }
+}
+
+cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d_world, const AdvectJob *d_jobs,
+                          int njobs, int nc, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  Grid3 G;
+  for (int a = 0; a < 3; ++a) {
+    G.n[a] = dims[a];
+    G.a0[a] = aabb[2 * a];
+    G.a1[a] = aabb[2 * a + 1];
+  }
+  const dim3 block(32, 4, 1);
+  const dim3 grid((dims[0] + 31) / 32, (dims[1] + 3) / 4, dims[2] * njobs);
+  advect_kernel<<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1], d_jobs, nc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st) {
+  wap_accumulate_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, vol, adv, alpha, gmax);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wap_accumulate_batch(const AccJob *d_jobs, int njobs, size_t n, double alpha, float gmax,
+                                        cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  const dim3 g((unsigned)((n + 255) / 256), njobs);
+  wap_accumulate_batch_kernel<<<g, 256, 0, st>>>(d_jobs, n, alpha, gmax);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_roi_floor(size_t n, float *vol, cudaStream_t st) {
+  roi_floor_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, vol);
+  return cudaGetLastError();
+}
+
+}  // namespace wap

@@ -1,0 +1,1043 @@
+// C ABI (include/wap/wap.h) of the GB300 warp-and-project library: the
+// context, its device arenas, and the host-side orchestration of PSART's
+// loops (WaP_Tomo.cpp:473-1678) and the flow solver's control flow
+// (optical_flow.h:409-828, 1002-1126) around the kernels.
+//
+// Device layout: the level's F frame volumes are one contiguous arena
+// (frame-major, CImg order inside a frame), likewise the flows (3 planar
+// channels per frame) and the CP state.  Independent frames are batched into
+// single launches (job tables), so a 64^3 frame set fills the GPU the way one
+// 256^3 frame does.  Nothing here falls back to the CPU: every numeric step
+// is a kernel in this library, and a missing GPU is an error.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "wap/wap.h"
+#include "wap_flow.h"
+#include "wap_geometry.h"
+#include "wap_internal.h"
+
+using namespace wap;
+
+namespace {
+
+struct DevMem {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevMem() = default;
+  DevMem(const DevMem &) = delete;
+  DevMem &operator=(const DevMem &) = delete;
+  ~DevMem() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b) {
+    if (b <= bytes && p) return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, b ? b : 16);
+    if (e == cudaSuccess) bytes = b;
+    else p = nullptr;
+    return e;
+  }
+  template <class T>
+  T *as() const {
+    return reinterpret_cast<T *>(p);
+  }
+};
+
+struct Status {
+  int code;
+};
+
+// Flow-solver workspace for one grid size (reused across pairs and calls).
+struct FlowWork {
+  int n[3] = {0, 0, 0};
+  DevMem va, vb, y, u, kty, kx4prev, warp, acc, err, world;
+  float aabb_key[6] = {0, 0, 0, 0, 0, 0};
+};
+
+// Multiscale pyramid buffers for one finest size.
+struct PyramidLevel {
+  int d[3];
+  DevMem i1, i2, v, y;
+};
+
+}  // namespace
+
+struct wap_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  wap_scan_desc scan{};
+  ScanGeometry sg{};
+  std::vector<double> angles;
+  std::vector<ProjGeom> h_geom;
+  DevMem geom;
+  float sd = 0.0f;
+  double halfW = 0.0, halfH = 0.0;
+  float gmax = 0.0f;
+  DevMem projs_own;
+  const float *projs = nullptr;
+  size_t np = 0, nv = 0;
+
+  // time level
+  int level = -1, F = 0;
+  std::vector<int> st, en;
+  std::vector<float> ft;
+  float tunit = 0.0f;
+  DevMem vols, flows, ytv, ytp, xbar, xprev, zero_vol;
+  DevMem dual, corr, warped, delta, back;
+  int maxwin = 0;
+
+  // job tables and scratch
+  DevMem jobs_fp, jobs_bp, jobs_adv, jobs_acc, jobs_misc;
+  DevMem world;  // cell-centre table of the scan grid
+  DevMem maxbits;
+  std::map<std::tuple<int, int, int>, std::unique_ptr<FlowWork>> flow_work;
+  std::vector<std::unique_ptr<PyramidLevel>> pyramid;
+  DevMem blur_a, blur_b, rs_a, rs_b;
+  std::map<std::pair<int, int>, std::unique_ptr<DevMem[]>> resize_tables;
+  DevMem cg_buf;
+
+  wap_stats stats{};
+  int profiling = 0;
+  std::vector<cudaEvent_t> pd_events;  // pairs, reused per 50-iteration chunk
+  std::string err;
+};
+
+namespace wap {
+cudaStream_t ctx_stream(wap_ctx *ctx) { return ctx->stream; }
+}  // namespace wap
+
+namespace {
+
+int fail(wap_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+#define CU(expr)                                                                                     \
+  do {                                                                                               \
+    cudaError_t _e = (expr);                                                                         \
+    if (_e != cudaSuccess) return fail(ctx, WAP_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+#define KL(expr)          \
+  do {                    \
+    CU(expr);             \
+    ++ctx->stats.kernel_launches; \
+  } while (0)
+
+#define CHECK(cond, code, msg)                \
+  do {                                        \
+    if (!(cond)) return fail(ctx, code, msg); \
+  } while (0)
+
+#define TRY(expr)             \
+  do {                        \
+    int _r = (expr);          \
+    if (_r != WAP_OK) return _r; \
+  } while (0)
+
+template <class T>
+int upload(wap_ctx *ctx, DevMem &m, const std::vector<T> &h) {
+  CU(m.ensure(sizeof(T) * h.size()));
+  if (!h.empty()) CU(cudaMemcpyAsync(m.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+  return WAP_OK;
+}
+
+float *vol_ptr(wap_ctx *c, int f) { return c->vols.as<float>() + (size_t)f * c->nv; }
+float *flow_ptr(wap_ctx *c, int f) { return c->flows.as<float>() + (size_t)f * 3 * c->nv; }
+
+void sart_order(int pstart, int pend, std::vector<int> &order) {
+  // front/back interleave of the window (WaP_Tomo.cpp:1449-1484).
+  const int num = pend - pstart + 1;
+  order.resize(num);
+  for (int i = 0; i < num; ++i) order[i] = (i % 2 == 0) ? pstart + i / 2 : pend - i / 2;
+}
+
+int ensure_level_buffers(wap_ctx *ctx) {
+  const size_t nv = ctx->nv, np = ctx->np, F = ctx->F;
+  CU(ctx->corr.ensure(sizeof(float) * F * np));
+  CU(ctx->dual.ensure(sizeof(float) * F * ctx->maxwin * np));
+  CU(ctx->warped.ensure(sizeof(float) * F * nv));
+  CU(ctx->delta.ensure(sizeof(float) * F * nv));
+  CU(ctx->back.ensure(sizeof(float) * F * nv));
+  return WAP_OK;
+}
+
+int roi_box(wap_ctx *ctx, int cut, int box[6]) {
+  // m_roi = cut * dims / level-0 dims (WaP_Tomo.cpp:529-536).
+  const int *d = ctx->scan.vol;
+  for (int a = 0; a < 3; ++a) {
+    const int r = (int)((float)cut * ((float)d[a] / (float)d[a]));
+    box[2 * a] = r;
+    box[2 * a + 1] = d[a] - r;
+  }
+  return WAP_OK;
+}
+
+// SART proximal operator on a set of frames at once (WaP_Tomo.cpp:1424-1678):
+// frames step through their windows in lock-step; each step is one batched
+// forward projection with the fused correction/dual epilogue and one batched
+// backprojection.
+int sart_frames(wap_ctx *ctx, const std::vector<int> &frames, int nb_sart, const int box[6], int exact) {
+  const size_t np = ctx->np;
+  const int W = ctx->scan.det[0], H = ctx->scan.det[1];
+  CU(cudaMemsetAsync(ctx->dual.p, 0, sizeof(float) * ctx->F * ctx->maxwin * np, ctx->stream));
+  std::vector<std::vector<int>> orders(frames.size());
+  int maxnum = 0;
+  for (size_t q = 0; q < frames.size(); ++q) {
+    const int f = frames[q];
+    sart_order(ctx->st[f], ctx->en[f], orders[q]);
+    maxnum = std::max(maxnum, (int)orders[q].size());
+  }
+  std::vector<FpJob> fp;
+  std::vector<BpJob> bp;
+  std::vector<int> step_off(maxnum + 1, 0);
+  for (int s = 0; s < maxnum; ++s) {
+    step_off[s] = (int)fp.size();
+    for (size_t q = 0; q < frames.size(); ++q) {
+      if (s >= (int)orders[q].size()) continue;
+      const int f = frames[q], pid = orders[q][s];
+      FpJob j{};
+      j.vol = vol_ptr(ctx, f);
+      j.proj = pid;
+      j.meas = ctx->projs;
+      j.dual = ctx->dual.as<float>() + ((size_t)f * ctx->maxwin + (pid - ctx->st[f])) * np;
+      j.corr = ctx->corr.as<float>() + (size_t)f * np;
+      fp.push_back(j);
+      BpJob b{};
+      b.vol = vol_ptr(ctx, f);
+      b.corr = j.corr;
+      b.proj = pid;
+      std::memcpy(b.box, box, sizeof(b.box));
+      bp.push_back(b);
+    }
+  }
+  step_off[maxnum] = (int)fp.size();
+  TRY(upload(ctx, ctx->jobs_fp, fp));
+  TRY(upload(ctx, ctx->jobs_bp, bp));
+  int mb[3] = {box[1] - box[0], box[3] - box[2], box[5] - box[4]};
+  for (int it = 1; it <= nb_sart; ++it)
+    for (int s = 0; s < maxnum; ++s) {
+      const int n = step_off[s + 1] - step_off[s];
+      KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_fp.as<FpJob>() + step_off[s], n, ctx->scan.vol, W, H,
+                        ctx->sd, ctx->scan.alpha, ctx->stream));
+      ctx->stats.fp_launches++;
+      ctx->stats.projections += n;
+      ctx->stats.backprojections += n;
+      KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_bp.as<BpJob>() + step_off[s], n, mb, ctx->scan.vol, W, H,
+                         ctx->halfW, ctx->halfH, (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha, ctx->gmax, 0,
+                         exact, ctx->stream));
+    }
+  // max(vol * imROI, 0) over the whole volume, imROI == 1 (WaP_Tomo.cpp:1646-1659).
+  bool contiguous = true;
+  for (size_t q = 0; q < frames.size(); ++q) contiguous = contiguous && frames[q] == frames[0] + (int)q;
+  if (contiguous && !frames.empty()) {
+    KL(launch_roi_floor(ctx->nv * frames.size(), vol_ptr(ctx, frames[0]), ctx->stream));
+  } else {
+    for (int f : frames) KL(launch_roi_floor(ctx->nv, vol_ptr(ctx, f), ctx->stream));
+  }
+  return WAP_OK;
+}
+
+int ensure_world(wap_ctx *ctx) {
+  const int *d = ctx->scan.vol;
+  if (ctx->world.p) return WAP_OK;
+  std::vector<float> h(d[0] + d[1] + d[2]);
+  const float aabb[6] = {0, (float)d[0], 0, (float)d[1], 0, (float)d[2]};
+  world_table(d, aabb, h.data());
+  return upload(ctx, ctx->world, h);
+}
+
+// Warp-and-project for a set of frames, each at its s-th window projection
+// (WaP_Tomo.cpp:796-822 driving WarpAndProjct, WaP_Tomo.cpp:1207-1421).
+struct WapItem {
+  int frame, proj;
+  float rtime;
+};
+
+int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
+  if (items.empty()) return WAP_OK;
+  TRY(ensure_world(ctx));
+  const size_t nv = ctx->nv, np = ctx->np;
+  const int W = ctx->scan.det[0], H = ctx->scan.det[1];
+  const int *d = ctx->scan.vol;
+  const float aabb[6] = {0, (float)d[0], 0, (float)d[1], 0, (float)d[2]};
+  const int nfames = ctx->F + 2;  // the level's frame list carries two padding copies
+  std::vector<AdvectJob> fwd, adj;
+  std::vector<FpJob> fp;
+  std::vector<BpJob> bp;
+  std::vector<AccJob> acc;
+  for (const WapItem &it : items) {
+    const int f = it.frame;
+    const int ff = it.rtime < 0.0f ? std::max(0, f - 1) : std::min(nfames - 1, f);
+    const int fa = std::max(0, f - 1);
+    // A frame without a computed flow uses a zero field (flows start at zero).
+    const float *vf = ff < ctx->F ? flow_ptr(ctx, ff) : ctx->zero_vol.as<float>();
+    AdvectJob a{vf, vol_ptr(ctx, f), ctx->warped.as<float>() + (size_t)f * nv, it.rtime};
+    fwd.push_back(a);
+    FpJob j{};
+    j.vol = a.out;
+    j.proj = it.proj;
+    j.meas = ctx->projs;
+    j.dual = nullptr;
+    j.corr = ctx->corr.as<float>() + (size_t)f * np;
+    fp.push_back(j);
+    BpJob b{};
+    b.vol = ctx->delta.as<float>() + (size_t)f * nv;
+    b.corr = j.corr;
+    b.proj = it.proj;
+    const int full[6] = {0, d[0], 0, d[1], 0, d[2]};
+    std::memcpy(b.box, full, sizeof(full));
+    bp.push_back(b);
+    AdvectJob r{flow_ptr(ctx, fa), b.vol, ctx->back.as<float>() + (size_t)f * nv, -it.rtime};
+    adj.push_back(r);
+    acc.push_back(AccJob{vol_ptr(ctx, f), r.out});
+  }
+  std::vector<AdvectJob> advs = fwd;
+  advs.insert(advs.end(), adj.begin(), adj.end());
+  TRY(upload(ctx, ctx->jobs_adv, advs));
+  TRY(upload(ctx, ctx->jobs_fp, fp));
+  TRY(upload(ctx, ctx->jobs_bp, bp));
+  TRY(upload(ctx, ctx->jobs_acc, acc));
+  const int n = (int)items.size();
+  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>(), n, 1, ctx->stream));
+  KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_fp.as<FpJob>(), n, d, W, H, ctx->sd, ctx->scan.alpha,
+                    ctx->stream));
+  ctx->stats.fp_launches++;
+  for (const WapItem &it : items)
+    CU(cudaMemsetAsync(ctx->delta.as<float>() + (size_t)it.frame * nv, 0, sizeof(float) * nv, ctx->stream));
+  int mb[3] = {d[0], d[1], d[2]};
+  KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_bp.as<BpJob>(), n, mb, d, W, H, ctx->halfW, ctx->halfH,
+                     (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha, ctx->gmax, 1, exact, ctx->stream));
+  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + n, n, 1, ctx->stream));
+  ctx->stats.advect_voxels += 2.0 * n * (double)nv;
+  ctx->stats.projections += n;
+  ctx->stats.backprojections += n;
+  KL(launch_wap_accumulate_batch(ctx->jobs_acc.as<AccJob>(), n, nv, ctx->scan.alpha, ctx->gmax, ctx->stream));
+  return WAP_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Flow
+// ---------------------------------------------------------------------------
+int resize_tables(wap_ctx *ctx, int Sin, int Sout, ResizeTables &tb) {
+  auto key = std::make_pair(Sin, Sout);
+  auto it = ctx->resize_tables.find(key);
+  if (it == ctx->resize_tables.end()) {
+    HostResizeAxis h = make_resize_axis(Sin, Sout);
+    std::unique_ptr<DevMem[]> m(new DevMem[5]);
+    TRY(upload(ctx, m[0], h.tap_start));
+    TRY(upload(ctx, m[1], h.tap_src));
+    TRY(upload(ctx, m[2], h.tap_w));
+    TRY(upload(ctx, m[3], h.base));
+    TRY(upload(ctx, m[4], h.frac));
+    it = ctx->resize_tables.emplace(key, std::move(m)).first;
+  }
+  tb.tap_start = it->second[0].as<int>();
+  tb.tap_src = it->second[1].as<int>();
+  tb.tap_w = it->second[2].as<float>();
+  tb.base = it->second[3].as<int>();
+  tb.frac = it->second[4].as<double>();
+  return WAP_OK;
+}
+
+int do_resize(wap_ctx *ctx, const int dims[3], int nc, const float *src, const int odims[3], float *out) {
+  const size_t big = (size_t)std::max(dims[0], odims[0]) * std::max(dims[1], odims[1]) *
+                     std::max(dims[2], odims[2]) * nc;
+  CU(ctx->rs_a.ensure(sizeof(float) * big));
+  CU(ctx->rs_b.ensure(sizeof(float) * big));
+  int cd[3] = {dims[0], dims[1], dims[2]};
+  int axes[3], na = 0;
+  for (int a = 0; a < 3; ++a)
+    if (dims[a] != odims[a]) axes[na++] = a;
+  if (na == 0) {
+    CU(cudaMemcpyAsync(out, src, sizeof(float) * dims[0] * dims[1] * dims[2] * nc, cudaMemcpyDeviceToDevice,
+                       ctx->stream));
+    return WAP_OK;
+  }
+  const float *in = src;
+  for (int q = 0; q < na; ++q) {
+    const int a = axes[q];
+    float *dst = (q == na - 1) ? out : ((q % 2 == 0) ? ctx->rs_a.as<float>() : ctx->rs_b.as<float>());
+    ResizeTables tb;
+    TRY(resize_tables(ctx, cd[a], odims[a], tb));
+    KL(launch_resize_axis(a, cd, nc, odims[a], tb, in, dst, ctx->stream));
+    cd[a] = odims[a];
+    in = dst;
+  }
+  return WAP_OK;
+}
+
+int do_blur(wap_ctx *ctx, const int dims[3], int nc, float sigma, const float *src, float *out) {
+  const size_t n = (size_t)dims[0] * dims[1] * dims[2] * nc;
+  const DericheCoefs k = deriche_coefs(sigma);
+  int axes[3], na = 0;
+  for (int a = 0; a < 3; ++a)
+    if (dims[a] > 1) axes[na++] = a;
+  if (k.skip || na == 0) {
+    CU(cudaMemcpyAsync(out, src, sizeof(float) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    return WAP_OK;
+  }
+  CU(ctx->blur_a.ensure(sizeof(float) * n));
+  CU(ctx->blur_b.ensure(sizeof(float) * n));
+  const float *in = src;
+  for (int q = 0; q < na; ++q) {
+    float *dst = (q == na - 1) ? out : ((q % 2 == 0) ? ctx->blur_a.as<float>() : ctx->blur_b.as<float>());
+    KL(launch_deriche(axes[q], dims, nc, k, in, dst, ctx->stream));
+    in = dst;
+  }
+  return WAP_OK;
+}
+
+FlowWork *flow_work(wap_ctx *ctx, const int dims[3]) {
+  auto key = std::make_tuple(dims[0], dims[1], dims[2]);
+  auto it = ctx->flow_work.find(key);
+  if (it != ctx->flow_work.end()) return it->second.get();
+  std::unique_ptr<FlowWork> w(new FlowWork);
+  const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
+  for (int a = 0; a < 3; ++a) w->n[a] = dims[a];
+  if (w->va.ensure(sizeof(float) * 3 * nv) || w->vb.ensure(sizeof(float) * 3 * nv) ||
+      w->y.ensure(sizeof(float) * 10 * nv) || w->u.ensure(sizeof(float) * 4 * nv) ||
+      w->kty.ensure(sizeof(float) * 3 * nv) || w->kx4prev.ensure(sizeof(float) * nv) ||
+      w->warp.ensure(sizeof(float) * nv) || w->acc.ensure(sizeof(double) * 2) || w->err.ensure(sizeof(float)) ||
+      w->world.ensure(sizeof(float) * (dims[0] + dims[1] + dims[2])))
+    return nullptr;
+  FlowWork *p = w.get();
+  ctx->flow_work.emplace(key, std::move(w));
+  return p;
+}
+
+// optical_flow::L1TVOpticalFlowNonlinear3D (optical_flow.h:88-995).
+// V (3 ch) is read and written whole; Y (10 ch: Y1,Y2,Y3,Y4) is read whole
+// and written on the ROI only, as the reference writes back.
+int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2, float *V, float *Y[4], float tol,
+               float lambda, int max_iters, int nwarps, const float aabb[6], const int roi6[6], int *iters_out,
+               long long *total) {
+  FlowWork *w = flow_work(ctx, dims);
+  CHECK(w, WAP_ENOMEM, "flow workspace allocation failed");
+  const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
+  FlowDims D;
+  for (int a = 0; a < 3; ++a) D.n[a] = dims[a];
+  for (int a = 0; a < 6; ++a) D.roi[a] = roi6[a];
+  // world table for this grid and box
+  if (std::memcmp(w->aabb_key, aabb, sizeof(w->aabb_key)) != 0 || !w->world.p) {
+    std::vector<float> h(dims[0] + dims[1] + dims[2]);
+    world_table(dims, aabb, h.data());
+    CU(cudaMemcpyAsync(w->world.p, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(w->aabb_key, aabb, sizeof(w->aabb_key));
+  }
+  float *vcur = w->va.as<float>(), *vnext = w->vb.as<float>();
+  float *y = w->y.as<float>();
+  CU(cudaMemcpyAsync(vcur, V, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(vnext, V, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
+  for (int q = 0; q < 3; ++q)
+    CU(cudaMemcpyAsync(y + 3 * q * nv, Y[q], sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(y + 9 * nv, Y[3], sizeof(float) * nv, cudaMemcpyDeviceToDevice, ctx->stream));
+  CU(cudaMemsetAsync(w->u.p, 0, sizeof(float) * 4 * nv, ctx->stream));
+  CU(cudaMemsetAsync(w->kty.p, 0, sizeof(float) * 3 * nv, ctx->stream));
+  const float sigma1 = std::min(1.0f / 3.0f, std::min(1.0f / 3.0f, 1.0f / 3.0f));
+  double *acc = w->acc.as<double>();
+  AdvectJob aj{vcur, I2, w->warp.as<float>(), -1.0f};
+  for (int wi = 0; wi < nwarps; ++wi) {
+    // advect I2 by the current flow, dt = -1 (optical_flow.h:418)
+    aj.vel = vcur;
+    std::vector<AdvectJob> ajs{aj};
+    TRY(upload(ctx, ctx->jobs_misc, ajs));
+    KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream));
+    ctx->stats.advect_voxels += (double)nv;
+    KL(launch_linearize(D, w->warp.as<float>(), I1, vcur, w->u.as<float>(), w->kx4prev.as<float>(), ctx->stream));
+    int it = 0;
+    float err = 1.0f;
+    // Profile only the largest grid seen in this outer iteration.
+    const bool prof = ctx->profiling && (long long)nv >= ctx->stats.pd_timed_voxels;
+    if (prof && (long long)nv > ctx->stats.pd_timed_voxels) {
+      ctx->stats.pd_timed_voxels = (long long)nv;
+      ctx->stats.ms_pd = 0.0;
+      ctx->stats.pd_timed = 0;
+    }
+    int pending = 0;
+    auto drain = [&]() -> int {
+      for (int q = 0; q < pending; ++q) {
+        float ms = 0.0f;
+        CU(cudaEventElapsedTime(&ms, ctx->pd_events[2 * q], ctx->pd_events[2 * q + 1]));
+        ctx->stats.ms_pd += ms;
+        ctx->stats.pd_timed++;
+      }
+      pending = 0;
+      return WAP_OK;
+    };
+    while (err > tol && it <= max_iters) {
+      ++it;
+      const int res = (it % 50 == 0);
+      const int store = ((it + 1) % 50 == 0);
+      if (res) CU(cudaMemsetAsync(acc, 0, sizeof(double) * 2, ctx->stream));
+      if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending], ctx->stream));
+      KL(launch_pd_primal(D, y, w->u.as<float>(), vcur, vnext, w->kty.as<float>(), store, res, acc, ctx->stream));
+      const int mode = (it == 1) ? (wi == 0 ? 1 : 2) : 0;
+      KL(launch_pd_dual(D, y, w->u.as<float>(), vnext, vcur, w->kx4prev.as<float>(), mode, lambda, sigma1, res,
+                        acc + 1, ctx->stream));
+      if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending++ + 1], ctx->stream));
+      std::swap(vcur, vnext);
+      if (res) {
+        KL(launch_residual_finish(acc, (int)nv, w->err.as<float>(), ctx->stream));
+        CU(cudaMemcpyAsync(&err, w->err.p, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+        TRY(drain());
+      }
+    }
+    if (pending) {
+      CU(cudaStreamSynchronize(ctx->stream));
+      TRY(drain());
+    }
+    ctx->stats.pd_voxel_iters += (double)it * (double)nv;
+    if (iters_out) iters_out[wi] = it;
+    if (total) *total += it;
+    ctx->stats.flow_pd_iterations += it;
+  }
+  CU(cudaMemcpyAsync(V, vcur, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
+  for (int q = 0; q < 3; ++q) KL(launch_roi_copy(D, 3, y + 3 * q * nv, Y[q], ctx->stream));
+  KL(launch_roi_copy(D, 1, y + 9 * nv, Y[3], ctx->stream));
+  return WAP_OK;
+}
+
+int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2, const float *V0, float tol,
+                    float lambda, int max_iters, int nwarps, float eta, float sigma, int scales, const int cut6[6],
+                    float *Vout, long long *total) {
+  CHECK(scales >= 1 && scales <= 16, WAP_EINVAL, "scales out of range");
+  const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
+  // blurred inputs live in the two finest-level image buffers' sources
+  std::vector<int> ld(3 * scales);
+  float t_eta = 1.0f;
+  for (int s = 0; s < scales; ++s) {
+    const int l = scales - 1 - s;  // coarse first
+    for (int a = 0; a < 3; ++a) ld[3 * l + a] = (int)(dims[a] * t_eta);
+    for (int a = 0; a < 3; ++a) CHECK(ld[3 * l + a] >= 3, WAP_EINVAL, "pyramid level smaller than 3 voxels");
+    t_eta = t_eta * eta;
+  }
+  if ((int)ctx->pyramid.size() < scales) ctx->pyramid.resize(scales);
+  for (int l = 0; l < scales; ++l) {
+    if (!ctx->pyramid[l]) ctx->pyramid[l].reset(new PyramidLevel);
+    PyramidLevel &P = *ctx->pyramid[l];
+    for (int a = 0; a < 3; ++a) P.d[a] = ld[3 * l + a];
+    const size_t m = (size_t)P.d[0] * P.d[1] * P.d[2];
+    CU(P.i1.ensure(sizeof(float) * m));
+    CU(P.i2.ensure(sizeof(float) * m));
+    CU(P.v.ensure(sizeof(float) * 3 * m));
+    CU(P.y.ensure(sizeof(float) * 10 * m));
+  }
+  // blur at full resolution, then build the pyramid (optical_flow.h:1010-1052)
+  PyramidLevel &fine = *ctx->pyramid[scales - 1];
+  DevMem b1, b2;
+  CU(b1.ensure(sizeof(float) * nv));
+  CU(b2.ensure(sizeof(float) * nv));
+  TRY(do_blur(ctx, dims, 1, sigma, I1, b1.as<float>()));
+  TRY(do_blur(ctx, dims, 1, sigma, I2, b2.as<float>()));
+  for (int l = 0; l < scales; ++l) {
+    PyramidLevel &P = *ctx->pyramid[l];
+    const size_t m = (size_t)P.d[0] * P.d[1] * P.d[2];
+    TRY(do_resize(ctx, dims, 1, b1.as<float>(), P.d, P.i1.as<float>()));
+    TRY(do_resize(ctx, dims, 1, b2.as<float>(), P.d, P.i2.as<float>()));
+    TRY(do_resize(ctx, dims, 3, V0, P.d, P.v.as<float>()));
+    CU(cudaMemsetAsync(P.y.p, 0, sizeof(float) * 10 * m, ctx->stream));
+  }
+  const float aabb[6] = {0, (float)dims[0], 0, (float)dims[1], 0, (float)dims[2]};
+  for (int l = 0; l < scales; ++l) {
+    PyramidLevel &P = *ctx->pyramid[l];
+    const size_t m = (size_t)P.d[0] * P.d[1] * P.d[2];
+    int roi[6];
+    for (int i = 0; i < 6; ++i) roi[i] = (float)cut6[i] * ((float)P.d[i / 2] / (float)dims[i / 2]);
+    float *Y[4] = {P.y.as<float>(), P.y.as<float>() + 3 * m, P.y.as<float>() + 6 * m, P.y.as<float>() + 9 * m};
+    TRY(flow_level(ctx, P.d, P.i1.as<float>(), P.i2.as<float>(), P.v.as<float>(), Y, tol, lambda, max_iters, nwarps,
+                   aabb, roi, nullptr, total));
+    if (l + 1 < scales) {
+      PyramidLevel &N = *ctx->pyramid[l + 1];
+      TRY(do_resize(ctx, P.d, 3, P.v.as<float>(), N.d, N.v.as<float>()));
+      TRY(do_resize(ctx, P.d, 10, P.y.as<float>(), N.d, N.y.as<float>()));
+    }
+  }
+  CU(cudaMemcpyAsync(Vout, fine.v.p, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));  // b1/b2 are released on return
+  return WAP_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_deg, int device) {
+  if (!out || !scan || !h_angles_deg) return WAP_EINVAL;
+  *out = nullptr;
+  for (int a = 0; a < 3; ++a)
+    if (scan->vol[a] < 3) return WAP_EINVAL;
+  if (scan->det[0] < 5 || scan->det[1] < 5 || scan->nproj < 1 || scan->nframes_cli < 1) return WAP_EINVAL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return WAP_ENODEV;
+  std::unique_ptr<wap_ctx> c(new wap_ctx);
+  wap_ctx *ctx = c.get();
+  ctx->device = device;
+  CU(cudaSetDevice(device));
+  CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  ctx->own_stream = true;
+  ctx->scan = *scan;
+  for (int a = 0; a < 3; ++a) ctx->sg.vol[a] = scan->vol[a];
+  ctx->sg.det[0] = scan->det[0];
+  ctx->sg.det[1] = scan->det[1];
+  ctx->sg.vs = scan->vs;
+  ctx->sg.ds = scan->ds;
+  ctx->sg.sid = scan->sid;
+  ctx->sg.sdd = scan->sdd;
+  for (int a = 0; a < 3; ++a) ctx->sg.oxyz[a] = scan->oxyz[a];
+  ctx->angles.assign(h_angles_deg, h_angles_deg + scan->nproj);
+  ctx->h_geom.resize(scan->nproj);
+  for (int p = 0; p < scan->nproj; ++p) ctx->h_geom[p] = projection_geometry(ctx->sg, ctx->angles[p]);
+  TRY(upload(ctx, ctx->geom, ctx->h_geom));
+  ctx->sd = sample_distance(scan->vs);
+  ctx->halfW = half_frustum(scan->det[0], scan->ds);
+  ctx->halfH = half_frustum(scan->det[1], scan->ds);
+  ctx->np = (size_t)scan->det[0] * scan->det[1];
+  ctx->nv = (size_t)scan->vol[0] * scan->vol[1] * scan->vol[2];
+  CU(ctx->maxbits.ensure(sizeof(unsigned)));
+  CU(ctx->zero_vol.ensure(sizeof(float) * 3 * ctx->nv));
+  CU(cudaMemsetAsync(ctx->zero_vol.p, 0, sizeof(float) * 3 * ctx->nv, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  *out = c.release();
+  return WAP_OK;
+}
+
+void wap_destroy(wap_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaStream_t s = ctx->own_stream ? ctx->stream : nullptr;
+  for (cudaEvent_t e : ctx->pd_events) cudaEventDestroy(e);
+  delete ctx;
+  if (s) cudaStreamDestroy(s);
+}
+
+const char *wap_last_error(const wap_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int wap_set_stream(wap_ctx *ctx, void *cuda_stream) {
+  CHECK(ctx, WAP_EINVAL, "null context");
+  if (ctx->own_stream && ctx->stream) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    cudaStreamDestroy(ctx->stream);
+  }
+  ctx->stream = (cudaStream_t)cuda_stream;
+  ctx->own_stream = false;
+  return WAP_OK;
+}
+
+int wap_synchronize(wap_ctx *ctx) {
+  CHECK(ctx, WAP_EINVAL, "null context");
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_get_stats(wap_ctx *ctx, wap_stats *out) {
+  CHECK(ctx && out, WAP_EINVAL, "null argument");
+  *out = ctx->stats;
+  return WAP_OK;
+}
+
+int wap_set_profiling(wap_ctx *ctx, int on) {
+  CHECK(ctx, WAP_EINVAL, "null context");
+  ctx->profiling = on ? 1 : 0;
+  if (ctx->profiling && ctx->pd_events.empty()) {
+    ctx->pd_events.resize(2 * 50);
+    for (auto &e : ctx->pd_events) CU(cudaEventCreate(&e));
+  }
+  return WAP_OK;
+}
+
+int wap_upload_projections(wap_ctx *ctx, const float *h_projs) {
+  CHECK(ctx && h_projs, WAP_EINVAL, "null argument");
+  const size_t n = ctx->np * ctx->scan.nproj;
+  CU(ctx->projs_own.ensure(sizeof(float) * n));
+  CU(cudaMemcpyAsync(ctx->projs_own.p, h_projs, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
+  ctx->projs = ctx->projs_own.as<float>();
+  // G_Max = max of the first projection image (projslevel[0][0], WaP_Tomo.cpp:347-348).
+  float m = h_projs[0];
+  for (size_t i = 1; i < ctx->np; ++i) m = h_projs[i] > m ? h_projs[i] : m;
+  ctx->gmax = m;
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_set_projections_device(wap_ctx *ctx, const float *d_projs) {
+  CHECK(ctx && d_projs, WAP_EINVAL, "null argument");
+  ctx->projs = d_projs;
+  KL(launch_max_reduce(d_projs, ctx->np, ctx->maxbits.as<unsigned>(), ctx->stream));
+  unsigned bits = 0;
+  CU(cudaMemcpyAsync(&bits, ctx->maxbits.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->gmax = decode_max_bits(bits);
+  return WAP_OK;
+}
+
+float wap_gmax(const wap_ctx *ctx) { return ctx ? ctx->gmax : 0.0f; }
+
+int wap_set_gmax(wap_ctx *ctx, float gmax) {
+  CHECK(ctx, WAP_EINVAL, "null context");
+  ctx->gmax = gmax;
+  return WAP_OK;
+}
+
+int wap_projection_geometry(const wap_scan_desc *scan, double angle_deg, float *h_p2m, float *h_m2v, float *h_mvv2m,
+                            float *h_eye) {
+  if (!scan || !h_p2m || !h_m2v || !h_mvv2m || !h_eye) return WAP_EINVAL;
+  ScanGeometry sg{};
+  for (int a = 0; a < 3; ++a) sg.vol[a] = scan->vol[a];
+  sg.det[0] = scan->det[0];
+  sg.det[1] = scan->det[1];
+  sg.vs = scan->vs;
+  sg.ds = scan->ds;
+  sg.sid = scan->sid;
+  sg.sdd = scan->sdd;
+  for (int a = 0; a < 3; ++a) sg.oxyz[a] = scan->oxyz[a];
+  const ProjGeom g = projection_geometry(sg, angle_deg);
+  std::memcpy(h_p2m, g.p2m, sizeof(g.p2m));
+  std::memcpy(h_m2v, g.m2v, sizeof(g.m2v));
+  std::memcpy(h_mvv2m, g.mvv2m, sizeof(g.mvv2m));
+  std::memcpy(h_eye, g.eye, sizeof(g.eye));
+  return WAP_OK;
+}
+
+int wap_level_frames(const wap_scan_desc *scan, int level, int *start, int *end, float *ftime, float *tunit, int cap) {
+  if (!scan || level < 0 || level > 4) return -WAP_EINVAL;
+  return level_frames(scan->nframes_cli, scan->nproj, level, start, end, ftime, tunit, cap);
+}
+
+int wap_level_setup(wap_ctx *ctx, int level) {
+  CHECK(ctx, WAP_EINVAL, "null context");
+  CHECK(level >= 0 && level <= 4, WAP_EINVAL, "level out of range");
+  const int F = level_frames(ctx->scan.nframes_cli, ctx->scan.nproj, level, nullptr, nullptr, nullptr, nullptr, 0);
+  ctx->st.assign(F, 0);
+  ctx->en.assign(F, 0);
+  ctx->ft.assign(F, 0.0f);
+  level_frames(ctx->scan.nframes_cli, ctx->scan.nproj, level, ctx->st.data(), ctx->en.data(), ctx->ft.data(),
+               &ctx->tunit, F);
+  ctx->level = level;
+  ctx->F = F;
+  ctx->maxwin = 0;
+  for (int f = 0; f < F; ++f) ctx->maxwin = std::max(ctx->maxwin, ctx->en[f] - ctx->st[f] + 1);
+  const size_t nv = ctx->nv;
+  CU(ctx->vols.ensure(sizeof(float) * F * nv));
+  CU(ctx->flows.ensure(sizeof(float) * F * 3 * nv));
+  CU(ctx->ytv.ensure(sizeof(float) * F * 3 * nv));
+  CU(ctx->ytp.ensure(sizeof(float) * F * nv));
+  CU(ctx->xbar.ensure(sizeof(float) * F * nv));
+  CU(ctx->xprev.ensure(sizeof(float) * F * nv));
+  CU(cudaMemsetAsync(ctx->vols.p, 0, sizeof(float) * F * nv, ctx->stream));
+  CU(cudaMemsetAsync(ctx->flows.p, 0, sizeof(float) * F * 3 * nv, ctx->stream));
+  CU(cudaMemsetAsync(ctx->ytv.p, 0, sizeof(float) * F * 3 * nv, ctx->stream));
+  CU(cudaMemsetAsync(ctx->ytp.p, 0, sizeof(float) * F * nv, ctx->stream));
+  CU(cudaMemsetAsync(ctx->xbar.p, 0, sizeof(float) * F * nv, ctx->stream));
+  CU(cudaMemsetAsync(ctx->xprev.p, 0, sizeof(float) * F * nv, ctx->stream));
+  TRY(ensure_level_buffers(ctx));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_level_nframes(const wap_ctx *ctx) { return ctx ? ctx->F : 0; }
+
+int wap_frame_volume_upload(wap_ctx *ctx, int frame, const float *h_vol) {
+  CHECK(ctx && h_vol, WAP_EINVAL, "null argument");
+  CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
+  CU(cudaMemcpyAsync(vol_ptr(ctx, frame), h_vol, sizeof(float) * ctx->nv, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_frame_volume_download(wap_ctx *ctx, int frame, float *h_vol) {
+  CHECK(ctx && h_vol, WAP_EINVAL, "null argument");
+  CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
+  CU(cudaMemcpyAsync(h_vol, vol_ptr(ctx, frame), sizeof(float) * ctx->nv, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_frame_flow_upload(wap_ctx *ctx, int frame, const float *h_flow) {
+  CHECK(ctx && h_flow, WAP_EINVAL, "null argument");
+  CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
+  CU(cudaMemcpyAsync(flow_ptr(ctx, frame), h_flow, sizeof(float) * 3 * ctx->nv, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_frame_flow_download(wap_ctx *ctx, int frame, float *h_flow) {
+  CHECK(ctx && h_flow, WAP_EINVAL, "null argument");
+  CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
+  CU(cudaMemcpyAsync(h_flow, flow_ptr(ctx, frame), sizeof(float) * 3 * ctx->nv, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+float *wap_frame_volume_device(wap_ctx *ctx, int frame) {
+  if (!ctx || frame < 0 || frame >= ctx->F) return nullptr;
+  return vol_ptr(ctx, frame);
+}
+
+float *wap_frame_flow_device(wap_ctx *ctx, int frame) {
+  if (!ctx || frame < 0 || frame >= ctx->F) return nullptr;
+  return flow_ptr(ctx, frame);
+}
+
+int wap_level_advance(wap_ctx *ctx) {
+  CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
+  const int F0 = ctx->F;
+  const size_t nv = ctx->nv;
+  DevMem old;
+  CU(old.ensure(sizeof(float) * F0 * nv));
+  CU(cudaMemcpyAsync(old.p, ctx->vols.p, sizeof(float) * F0 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
+  TRY(wap_level_setup(ctx, ctx->level + 1));
+  for (int i = 0; i < F0; ++i)
+    for (int k = 0; k < 2; ++k)
+      if (2 * i + k < ctx->F)
+        CU(cudaMemcpyAsync(vol_ptr(ctx, 2 * i + k), old.as<float>() + (size_t)i * nv, sizeof(float) * nv,
+                           cudaMemcpyDeviceToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_forward_project(wap_ctx *ctx, int proj, const float *d_vol, float *d_img, float *d_len, float *d_weight) {
+  return wap_forward_project_batch(ctx, 1, &proj, &d_vol, &d_img, &d_len, &d_weight);
+}
+
+int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const float *const *h_d_vols,
+                              float *const *h_d_imgs, float *const *h_d_lens, float *const *h_d_weights) {
+  CHECK(ctx && h_proj && h_d_vols, WAP_EINVAL, "null argument");
+  CHECK(njobs >= 1 && njobs <= 65535, WAP_EINVAL, "job count out of range");
+  std::vector<FpJob> jobs(njobs);
+  for (int q = 0; q < njobs; ++q) {
+    CHECK(h_proj[q] >= 0 && h_proj[q] < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
+    CHECK(h_d_vols[q], WAP_EINVAL, "null volume");
+    FpJob j{};
+    j.vol = h_d_vols[q];
+    j.proj = h_proj[q];
+    j.img = h_d_imgs ? h_d_imgs[q] : nullptr;
+    j.len = h_d_lens ? h_d_lens[q] : nullptr;
+    j.weight = h_d_weights ? h_d_weights[q] : nullptr;
+    jobs[q] = j;
+  }
+  TRY(upload(ctx, ctx->jobs_misc, jobs));
+  KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_misc.as<FpJob>(), njobs, ctx->scan.vol, ctx->scan.det[0],
+                    ctx->scan.det[1], ctx->sd, ctx->scan.alpha, ctx->stream));
+  ctx->stats.fp_launches++;
+  return WAP_OK;
+}
+
+int wap_correction(wap_ctx *ctx, int n, const float *d_meas, const float *d_img, const float *d_len, float *d_dual,
+                   float *d_corr) {
+  CHECK(ctx && d_meas && d_img && d_len && d_corr, WAP_EINVAL, "null argument");
+  KL(launch_correction(n, d_meas, d_img, d_len, d_dual, ctx->scan.alpha, d_corr, ctx->stream));
+  return WAP_OK;
+}
+
+int wap_backproject_voxel(wap_ctx *ctx, int proj, const float *d_corr, const int *box, int mode, int exact,
+                          float *d_vol) {
+  CHECK(ctx && d_corr && box && d_vol, WAP_EINVAL, "null argument");
+  CHECK(proj >= 0 && proj < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
+  CHECK(mode == 0 || mode == 1, WAP_EINVAL, "mode must be 0 or 1");
+  for (int a = 0; a < 3; ++a)
+    CHECK(box[2 * a] >= 0 && box[2 * a + 1] <= ctx->scan.vol[a] && box[2 * a] <= box[2 * a + 1], WAP_EINVAL,
+          "box outside the volume");
+  BpJob b{};
+  b.vol = d_vol;
+  b.corr = d_corr;
+  b.proj = proj;
+  std::memcpy(b.box, box, sizeof(b.box));
+  std::vector<BpJob> jobs{b};
+  TRY(upload(ctx, ctx->jobs_misc, jobs));
+  int mb[3] = {box[1] - box[0], box[3] - box[2], box[5] - box[4]};
+  KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_misc.as<BpJob>(), 1, mb, ctx->scan.vol, ctx->scan.det[0],
+                     ctx->scan.det[1], ctx->halfW, ctx->halfH, (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha,
+                     ctx->gmax, mode, exact, ctx->stream));
+  return WAP_OK;
+}
+
+int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_contrib, float *d_weight) {
+  CHECK(ctx && d_corr && d_contrib && d_weight, WAP_EINVAL, "null argument");
+  CHECK(proj >= 0 && proj < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
+  std::vector<SplatJob> jobs{SplatJob{d_corr, proj, d_contrib, d_weight}};
+  TRY(upload(ctx, ctx->jobs_misc, jobs));
+  KL(launch_ray_splat(ctx->geom.as<ProjGeom>(), ctx->jobs_misc.as<SplatJob>(), 1, ctx->scan.vol, ctx->scan.det[0],
+                      ctx->scan.det[1], ctx->sd, ctx->stream));
+  return WAP_OK;
+}
+
+int wap_advect(wap_ctx *ctx, const int *dims, const float *aabb, const float *d_vel, const float *d_src, int nc,
+               float dt, float *d_out) {
+  CHECK(ctx && dims && aabb && d_vel && d_src && d_out, WAP_EINVAL, "null argument");
+  CHECK(dims[0] >= 3 && dims[1] >= 3 && dims[2] >= 3 && nc >= 1, WAP_EINVAL, "grid must be at least 3^3");
+  CHECK(aabb[1] > aabb[0] && aabb[3] > aabb[2] && aabb[5] > aabb[4], WAP_EINVAL, "empty bounding box");
+  std::vector<float> h(dims[0] + dims[1] + dims[2]);
+  world_table(dims, aabb, h.data());
+  DevMem tab;
+  TRY(upload(ctx, tab, h));
+  std::vector<AdvectJob> jobs{AdvectJob{d_vel, d_src, d_out, dt}};
+  TRY(upload(ctx, ctx->jobs_misc, jobs));
+  KL(launch_advect(dims, aabb, tab.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, nc, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));  // the table is released on return
+  return WAP_OK;
+}
+
+int wap_blur(wap_ctx *ctx, const int *dims, int nc, float sigma, const float *d_src, float *d_out) {
+  CHECK(ctx && dims && d_src && d_out, WAP_EINVAL, "null argument");
+  return do_blur(ctx, dims, nc, sigma, d_src, d_out);
+}
+
+int wap_resize(wap_ctx *ctx, const int *dims, int nc, const float *d_src, const int *odims, float *d_out) {
+  CHECK(ctx && dims && odims && d_src && d_out, WAP_EINVAL, "null argument");
+  for (int a = 0; a < 3; ++a) CHECK(dims[a] >= 1 && odims[a] >= 1, WAP_EINVAL, "empty grid");
+  return do_resize(ctx, dims, nc, d_src, odims, d_out);
+}
+
+int wap_flow_level(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, float *d_V, float *d_Y1,
+                   float *d_Y2, float *d_Y3, float *d_Y4, float tol, float lambda, int max_iters, int nwarps,
+                   const float *aabb, const int *roi6, int *h_iters) {
+  CHECK(ctx && dims && d_I1 && d_I2 && d_V && d_Y1 && d_Y2 && d_Y3 && d_Y4 && aabb && roi6, WAP_EINVAL,
+        "null argument");
+  CHECK(dims[0] >= 3 && dims[1] >= 3 && dims[2] >= 3, WAP_EINVAL, "grid must be at least 3^3");
+  float *Y[4] = {d_Y1, d_Y2, d_Y3, d_Y4};
+  TRY(flow_level(ctx, dims, d_I1, d_I2, d_V, Y, tol, lambda, max_iters, nwarps, aabb, roi6, h_iters, nullptr));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_flow_multiscale(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, const float *d_V0,
+                        float tol, float lambda, int max_iters, int nwarps, float eta, float sigma, int scales,
+                        const int *cut6, float *d_Vout, long long *h_total_iters) {
+  CHECK(ctx && dims && d_I1 && d_I2 && d_V0 && cut6 && d_Vout, WAP_EINVAL, "null argument");
+  long long tot = 0;
+  TRY(flow_multiscale(ctx, dims, d_I1, d_I2, d_V0, tol, lambda, max_iters, nwarps, eta, sigma, scales, cut6, d_Vout,
+                      &tot));
+  if (h_total_iters) *h_total_iters = tot;
+  return WAP_OK;
+}
+
+int wap_sart_prox(wap_ctx *ctx, int frame, int nb_sart, int cut, int exact) {
+  CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
+  CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
+  CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
+  int box[6];
+  roi_box(ctx, cut, box);
+  std::vector<int> frames{frame};
+  TRY(sart_frames(ctx, frames, nb_sart, box, exact));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exact) {
+  CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
+  CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
+  CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
+  CHECK(proj >= 0 && proj < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
+  std::vector<WapItem> items{WapItem{frame, proj, rtime}};
+  TRY(wap_step(ctx, items, exact));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1, wap_stats *stats) {
+  CHECK(ctx && sch, WAP_EINVAL, "null argument");
+  CHECK(ctx->level >= 0, WAP_ESTATE, "no level set up");
+  CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
+  CHECK(0 <= f0 && f0 < f1 && f1 <= ctx->F, WAP_EINVAL, "frame range out of bounds");
+  CHECK(sch->cut >= 1 && 2 * sch->cut < ctx->scan.vol[0] && 2 * sch->cut < ctx->scan.vol[1] &&
+            2 * sch->cut < ctx->scan.vol[2],
+        WAP_EINVAL, "cut must leave a non-empty ROI and be at least 1");
+  CHECK(sch->n_cp >= 0 && sch->nb_sart >= 0 && sch->nb_projwarp >= 0 && sch->flow_iters >= 0 &&
+            sch->flow_warps >= 0 && sch->flow_scales >= 1,
+        WAP_EINVAL, "negative schedule count");
+  ctx->stats = wap_stats{};
+  ctx->stats.flow_pd_iterations = 0;
+  const int F = ctx->F;
+  int box[6];
+  roi_box(ctx, sch->cut, box);
+  cudaEvent_t ev[4];
+  for (auto &e : ev) CU(cudaEventCreate(&e));
+  CU(cudaEventRecord(ev[0], ctx->stream));
+  // (1) CP prior + SART proximal steps (WaP_Tomo.cpp:563-698)
+  CpArgs ca;
+  for (int a = 0; a < 3; ++a) ca.n[a] = ctx->scan.vol[a];
+  std::memcpy(ca.box, box, sizeof(box));
+  ca.f0 = f0;
+  ca.F = f1 - f0;
+  ca.Ftot = F;
+  ca.sigma = (float)(.9 / (8.0f * 1.0f));
+  ca.tau = 1.0f;
+  ca.tv_w = (float)ctx->scan.tv_w;
+  ca.tp_w = (float)ctx->scan.tp_w;
+  ca.gmax = ctx->gmax;
+  std::vector<int> frames;
+  for (int f = f0; f < f1; ++f) frames.push_back(f);
+  for (int icp = 1; icp <= sch->n_cp; ++icp) {
+    KL(launch_cp_dual(ca, ctx->xbar.as<float>(), ctx->zero_vol.as<float>(), ctx->ytv.as<float>(),
+                      ctx->ytp.as<float>(), ctx->stream));
+    KL(launch_cp_primal(ca, ctx->ytp.as<float>(), ctx->ytv.as<float>(), ctx->vols.as<float>(), ctx->xprev.as<float>(),
+                        ctx->stream));
+    TRY(sart_frames(ctx, frames, sch->nb_sart, box, sch->bp_exact));
+    KL(launch_cp_overrelax(ca, ctx->vols.as<float>(), ctx->xprev.as<float>(), ctx->xbar.as<float>(), ctx->stream));
+    ctx->stats.cp_frame_passes += ca.F;
+  }
+  CU(cudaEventRecord(ev[1], ctx->stream));
+  // (2) flow for each adjacent pair (WaP_Tomo.cpp:732-777)
+  const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
+  long long total = 0;
+  for (int f = f0; f < f1 && f + 1 < F; ++f)
+    TRY(flow_multiscale(ctx, ctx->scan.vol, vol_ptr(ctx, f), vol_ptr(ctx, f + 1), flow_ptr(ctx, f), sch->flow_tol,
+                        sch->flow_lambda, sch->flow_iters, sch->flow_warps, sch->flow_eta, sch->flow_sigma,
+                        sch->flow_scales, cut6, flow_ptr(ctx, f), &total));
+  CU(cudaEventRecord(ev[2], ctx->stream));
+  // (3) warp-and-project over each visited frame's window (WaP_Tomo.cpp:796-822)
+  const int wend = std::min(f1, std::min(sch->wp_frames, F));
+  int maxnum = 0;
+  for (int f = f0; f < wend; ++f) maxnum = std::max(maxnum, ctx->en[f] - ctx->st[f] + 1);
+  for (int wp = 0; wp < sch->nb_projwarp; ++wp)
+    for (int s = 0; s < maxnum; ++s) {
+      std::vector<WapItem> items;
+      for (int f = f0; f < wend; ++f) {
+        const int ik = ctx->st[f] + s;
+        if (ik > ctx->en[f]) continue;
+        float td = (ik - ctx->ft[f]) / ctx->tunit;
+        td = mac_min(mac_max(-1.0f, td), 1.0f);
+        items.push_back(WapItem{f, ik, td});
+      }
+      TRY(wap_step(ctx, items, sch->bp_exact));
+    }
+  CU(cudaEventRecord(ev[3], ctx->stream));
+  CU(cudaEventSynchronize(ev[3]));
+  float ms[3];
+  for (int q = 0; q < 3; ++q) CU(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
+  for (auto &e : ev) cudaEventDestroy(e);
+  ctx->stats.ms_cp = ms[0];
+  ctx->stats.ms_flow = ms[1];
+  ctx->stats.ms_wap = ms[2];
+  if (stats) *stats = ctx->stats;
+  return WAP_OK;
+}
+
+int wap_outer_iteration(wap_ctx *ctx, const wap_schedule *sch, wap_stats *stats) {
+  CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
+  return wap_outer_iteration_frames(ctx, sch, 0, ctx->F, stats);
+}
+
+}  // extern "C"

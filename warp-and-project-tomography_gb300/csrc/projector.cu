@@ -1,0 +1,389 @@
+// Cone-beam projector kernels: ray-driven forward projection (with the fused
+// PSART correction epilogue), the voxel-driven bicubic backprojection, and
+// the ray-driven matched backprojection (splat).
+//
+// Forward projection restates GenerateImage_MT / ProduceRay / CastingRay /
+// T_VolumeAccess::GetScalarValue (TypicalRayProducer.core.h:32-225,
+// RayCaster.core.h:42-188, SingleScalarVolume.core.h:66-202) one thread per
+// detector pixel: the reference's march accumulates t and pos in float and
+// re-derives t at every block boundary, so the sample positions (and with them
+// the sample counts) are a sequential recurrence that must be replayed, not
+// reformulated.  Each warp owns an 8x4 pixel patch so the warp's 32 rays stay
+// within a few voxels of each other and the trilinear gathers hit L1.
+#include <cstring>
+
+#include "wap_internal.h"
+
+namespace wap {
+namespace {
+
+struct VolView {
+  const float *__restrict__ d;
+  int nx, ny, nz;
+  __device__ __forceinline__ float at(int x, int y, int z) const {
+    // T_VolumeAccess::GetScalarValue(int,int,int): clamp each index to [0, n-1].
+    x = mac_maxi(mac_mini(x, nx - 1), 0);
+    y = mac_maxi(mac_mini(y, ny - 1), 0);
+    z = mac_maxi(mac_mini(z, nz - 1), 0);
+    return __ldg(d + (x + nx * (y + ny * z)));
+  }
+};
+
+// Trilinear sample with the reference's clamp-then-truncate (SingleScalarVolume.core.h:99-202).
+struct TrilinearSampler {
+  VolView v;
+  float sumw;
+  __device__ __forceinline__ float operator()(float p0, float p1, float p2) {
+    p0 = mac_max(mac_min(p0, (float)(v.nx - 1)), 0.0f);
+    p1 = mac_max(mac_min(p1, (float)(v.ny - 1)), 0.0f);
+    p2 = mac_max(mac_min(p2, (float)(v.nz - 1)), 0.0f);
+    const int i = (int)p0, j = (int)p1, k = (int)p2;
+    float f2 = p0 - (float)i;
+    float f1 = 1.0f - f2;
+    sumw += 1.0f;
+    float a = v.at(i, j, k) * f1 + v.at(i + 1, j, k) * f2;
+    float b = v.at(i, j + 1, k) * f1 + v.at(i + 1, j + 1, k) * f2;
+    float c = v.at(i, j, k + 1) * f1 + v.at(i + 1, j, k + 1) * f2;
+    float d = v.at(i, j + 1, k + 1) * f1 + v.at(i + 1, j + 1, k + 1) * f2;
+    f2 = p1 - (float)j;
+    f1 = 1.0f - f2;
+    a = a * f1 + b * f2;
+    c = c * f1 + d * f2;
+    f2 = p2 - (float)k;
+    f1 = 1.0f - f2;
+    return a * f1 + c * f2;
+  }
+};
+
+// Back-projection mode of the same sampler (SingleScalarVolume.core.h:85-96,
+// 149-199): splat corr*w_k and w_k onto the 8 taps.  Taps past the last voxel
+// carry weight 0 (the position is clamped to n-1) and are dropped.
+struct SplatSampler {
+  int nx, ny, nz;
+  float corr;
+  float *__restrict__ contrib;
+  float *__restrict__ weight;
+  float sumw;
+  __device__ __forceinline__ float operator()(float p0, float p1, float p2) {
+    p0 = mac_max(mac_min(p0, (float)(nx - 1)), 0.0f);
+    p1 = mac_max(mac_min(p1, (float)(ny - 1)), 0.0f);
+    p2 = mac_max(mac_min(p2, (float)(nz - 1)), 0.0f);
+    const int i = (int)p0, j = (int)p1, k = (int)p2;
+    const float t0 = p0 - (float)i, t1 = p1 - (float)j, t2 = p2 - (float)k;
+    const float M0 = 1.0f - t0, M1 = 1.0f - t1, M2 = 1.0f - t2;
+    const float w[8] = {M0 * M1 * M2, t0 * M1 * M2, M0 * t1 * M2, t0 * t1 * M2,
+                        M0 * M1 * t2, t0 * M1 * t2, M0 * t1 * t2, t0 * t1 * t2};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int x = i + (c & 1), y = j + ((c >> 1) & 1), z = k + ((c >> 2) & 1);
+      if (x >= nx || y >= ny || z >= nz) continue;
+      const int id = x + nx * (y + ny * z);
+      atomicAdd(contrib + id, corr * w[c]);
+      atomicAdd(weight + id, w[c]);
+    }
+    return 0.0f;
+  }
+};
+
+// ProduceRay (TypicalRayProducer.core.h:32-120).
+__device__ __forceinline__ void produce_ray(const ProjGeom &g, int nx, int ny, int nz, float px, float py,
+                                            float vz[4], float vu[4], float &tnear, float &tfar) {
+  float mp[4];
+  mat4_vec(g.p2m, px, py, 0.0f, 1.0f, mp);
+  const float inv = 1.0f / mp[3];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) mp[a] *= inv;
+  float dir[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) dir[a] = mp[a] - g.eye[a];
+  const float li = 1.0f / sqrtf(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+  dir[0] *= li;
+  dir[1] *= li;
+  dir[2] *= li;
+  mat4_vec(g.m2v, g.eye[0], g.eye[1], g.eye[2], g.eye[3], vz);
+  mat4_vec(g.m2v, dir[0], dir[1], dir[2], dir[3], vu);
+  const float hi[3] = {(float)(nx - 1), (float)(ny - 1), (float)(nz - 1)};
+  float tmn[3], tmx[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float t1 = (0.0f - vz[a]) / vu[a];
+    const float t2 = (hi[a] - vz[a]) / vu[a];
+    tmn[a] = mac_min(t1, t2);
+    tmx[a] = mac_max(t1, t2);
+  }
+  tnear = mac_max(mac_max(tmn[0], tmn[1]), tmn[2]);
+  tnear = mac_max(tnear, 0.0f);
+  tfar = mac_min(mac_min(tmx[0], tmx[1]), tmx[2]);
+}
+
+// CastingRay with one block spanning the whole volume (RayCasterPrepare sets
+// bsize = volume dims, RayCaster.core.h:191-207).
+template <class Sampler>
+__device__ __forceinline__ float cast_ray(Sampler &smp, const int n[3], const float vz[4], const float vu[4],
+                                          float tnear, float tfar, float sd) {
+  float density = 0.0f;
+  float t1 = tnear;
+  const float pos1[3] = {vz[0] + vu[0] * t1, vz[1] + vu[1] * t1, vz[2] + vu[2] * t1};
+  const float step[3] = {vu[0] * sd, vu[1] * sd, vu[2] * sd};
+  density += smp(pos1[0], pos1[1], pos1[2]) * sd;
+  float tMax[3], tDelta[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const int bs = n[a];
+    if (vu[a] == 0.0f) {
+      tMax[a] = tfar;
+    } else if (vu[a] < 0.0f) {
+      const int blk = ((int)ceilf(pos1[a] - 0.5f) - 1) / bs;
+      tMax[a] = ((float)(blk * bs) + 0.5f - vz[a]) / vu[a];
+      tDelta[a] = (float)(-(1 * bs)) / vu[a];
+    } else {
+      const int blk = ((int)floorf(pos1[a] - 0.5f)) / bs;
+      tMax[a] = ((float)((blk + 1) * bs) + 0.5f - vz[a]) / vu[a];
+      tDelta[a] = (float)(1 * bs) / vu[a];
+    }
+  }
+  while (t1 < tfar) {
+    float tb = mac_min(mac_min(tMax[0], tMax[1]), tMax[2]);
+    if (tb > tfar) tb = tfar;
+    float t = ceilf((t1 - tnear) / sd) * sd + tnear;
+    float p0 = vz[0] + vu[0] * t, p1 = vz[1] + vu[1] * t, p2 = vz[2] + vu[2] * t;
+    while (t < tb) {
+      density += smp(p0, p1, p2) * sd;
+      t += sd;
+      p0 += step[0];
+      p1 += step[1];
+      p2 += step[2];
+    }
+    if (tMax[0] < tMax[1]) {
+      if (tMax[0] < tMax[2]) tMax[0] += tDelta[0];
+      else tMax[2] += tDelta[2];
+    } else {
+      if (tMax[1] < tMax[2]) tMax[1] += tDelta[1];
+      else tMax[2] += tDelta[2];
+    }
+    t1 = tb;
+  }
+  return density;
+}
+
+// 16x8 pixel tile per 128-thread block, each warp an 8x4 patch.
+__device__ __forceinline__ void tile_pixel(int &i, int &j) {
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  i = blockIdx.x * 16 + (w & 1) * 8 + (lane & 7);
+  j = blockIdx.y * 8 + (w >> 1) * 4 + (lane >> 3);
+}
+
+__global__ void __launch_bounds__(128) fp_kernel(const ProjGeom *__restrict__ geom, const FpJob *__restrict__ jobs,
+                                                 int nx, int ny, int nz, int W, int H, float sd, double alpha) {
+  int i, j;
+  tile_pixel(i, j);
+  if (i >= W || j >= H) return;
+  const FpJob job = jobs[blockIdx.z];
+  const ProjGeom &g = geom[job.proj];
+  const int n[3] = {nx, ny, nz};
+  float vz[4], vu[4], tn, tf;
+  produce_ray(g, nx, ny, nz, (float)i, (float)j, vz, vu, tn, tf);
+  TrilinearSampler smp{VolView{job.vol, nx, ny, nz}, 0.0f};
+  float value = 0.0f, len = 0.0f;
+  if (tn < tf) {
+    len = tf - tn;
+    value = cast_ray(smp, n, vz, vu, tn, tf, sd);
+  }
+  const int k = i + j * W;
+  if (job.img) job.img[k] = value;
+  if (job.len) job.len[k] = len;
+  if (job.weight) job.weight[k] = smp.sumw;
+  if (job.meas) {
+    // PSART correction and dual (WaP_Tomo.cpp:1530-1555, Factor = 1).
+    const size_t off = (size_t)job.proj * W * H;
+    const float y = job.dual ? job.dual[k] : 0.0f;
+    const float p = __ldg(job.meas + off + k);
+    const float c = (float)(1.0f * p - 1.0f * value - y) / (float)(1.0f * len + 1.0f);
+    job.corr[k] = c;
+    if (job.dual) job.dual[k] = (float)((double)y + alpha * (double)c);
+  }
+}
+
+__global__ void __launch_bounds__(128) splat_kernel(const ProjGeom *__restrict__ geom,
+                                                    const SplatJob *__restrict__ jobs, int nx, int ny, int nz, int W,
+                                                    int H, float sd) {
+  int i, j;
+  tile_pixel(i, j);
+  if (i >= W || j >= H) return;
+  const SplatJob job = jobs[blockIdx.z];
+  const ProjGeom &g = geom[job.proj];
+  const int n[3] = {nx, ny, nz};
+  float vz[4], vu[4], tn, tf;
+  produce_ray(g, nx, ny, nz, (float)i, (float)j, vz, vu, tn, tf);
+  if (!(tn < tf)) return;
+  SplatSampler smp{nx, ny, nz, __ldg(job.corr + i + j * W), job.contrib, job.weight, 0.0f};
+  cast_ray(smp, n, vz, vu, tn, tf, sd);
+}
+
+__global__ void correction_kernel(int n, const float *__restrict__ meas, const float *__restrict__ img,
+                                  const float *__restrict__ len, float *dual, double alpha, float *corr) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float y = dual ? dual[k] : 0.0f;
+  const float c = (float)(1.0f * meas[k] - 1.0f * img[k] - y) / (float)(1.0f * len[k] + 1.0f);
+  corr[k] = c;
+  if (dual) dual[k] = (float)((double)y + alpha * (double)c);
+}
+
+// ---------------------------------------------------------------------------
+// Voxel-driven bicubic backprojection (WaP_Tomo.cpp:208-222, 1557-1628 and
+// 1294-1374).  One thread per voxel; the 16 taps come from the correction
+// image, which every block of a launch shares (L1/L2 resident).
+// ---------------------------------------------------------------------------
+
+// cubicInterpolate evaluated as the reference does: the float differences
+// p2-p0 and p1-p2 first, everything else in double (the literals are double).
+__device__ __forceinline__ float cubic_exact(float p0, float p1, float p2, float p3, float x) {
+  const double xd = x;
+  const double inner = 3.0 * (double)(p1 - p2) + (double)p3 - (double)p0;
+  const double mid = 2.0 * (double)p0 - 5.0 * (double)p1 + 4.0 * (double)p2 - (double)p3 + xd * inner;
+  const double outer = (double)(p2 - p0) + xd * mid;
+  return (float)((double)p1 + 0.5 * xd * outer);
+}
+
+// The same Catmull-Rom polynomial in FP32 with fused multiply-adds.
+__device__ __forceinline__ float cubic_fast(float p0, float p1, float p2, float p3, float x) {
+  const float inner = __fmaf_rn(3.0f, p1 - p2, p3 - p0);
+  const float mid = __fmaf_rn(x, inner, __fmaf_rn(2.0f, p0, __fmaf_rn(-5.0f, p1, __fmaf_rn(4.0f, p2, -p3))));
+  const float outer = __fmaf_rn(x, mid, p2 - p0);
+  return __fmaf_rn(0.5f * x, outer, p1);
+}
+
+template <bool kExact, int kMode>
+__global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restrict__ geom,
+                                                       const BpJob *__restrict__ jobs, int zblocks, int nx, int ny,
+                                                       int W, int H, double halfW, double halfH, float sdd,
+                                                       double ds, int float_ok, double alpha, float gmax) {
+  const int jb = blockIdx.z / zblocks;
+  const BpJob job = jobs[jb];
+  const int x = job.box[0] + blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = job.box[2] + blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = job.box[4] + (blockIdx.z % zblocks) * blockDim.z + threadIdx.z;
+  if (x >= job.box[1] || y >= job.box[3] || z >= job.box[5]) return;
+  const ProjGeom &g = geom[job.proj];
+  float det[4];
+  mat4_vec(g.mvv2m, (float)x, (float)y, (float)z, 1.0f, det);
+  const float qx = (det[0] / det[2]) * sdd;
+  const float qy = (det[1] / det[2]) * sdd;
+  float _px, _py;
+  if (float_ok) {
+    // halfW, halfH and ds are exact floats here, and a single double
+    // operation rounded to float equals the float operation.
+    _px = (float)halfW - qx;
+    _py = (float)halfH - qy;
+    _px = _px / (float)ds;
+    _py = _py / (float)ds;
+  } else {
+    _px = (float)(halfW - (double)qx);
+    _py = (float)(halfH - (double)qy);
+    _px = (float)((double)_px / ds);
+    _py = (float)((double)_py / ds);
+  }
+  const int px = (int)_px, py = (int)_py;
+  const float dx = _px - (float)px, dy = _py - (float)py;
+  if (px < 2 || px >= W - 2 || py < 2 || py >= H - 2) return;
+  const float *__restrict__ pC = job.corr + py * W + px;
+  float arr[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float *c = pC + (r - 1);
+    const float a0 = __ldg(c - W), a1 = __ldg(c), a2 = __ldg(c + W), a3 = __ldg(c + 2 * W);
+    arr[r] = kExact ? cubic_exact(a0, a1, a2, a3, dy) : cubic_fast(a0, a1, a2, a3, dy);
+  }
+  const float gv = kExact ? cubic_exact(arr[0], arr[1], arr[2], arr[3], dx)
+                          : cubic_fast(arr[0], arr[1], arr[2], arr[3], dx);
+  float *v = job.vol + (x + nx * (y + ny * z));
+  if (kMode == 0) {
+    float nv = kExact ? (float)((double)*v + alpha * (double)gv) : __fmaf_rn((float)alpha, gv, *v);
+    nv = mac_max(mac_min(gmax, nv), 0.0f);
+    *v = nv;
+  } else {
+    *v = *v + gv;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_forward(const ProjGeom *d_geom, const FpJob *d_jobs, int njobs, const int dims[3], int W, int H,
+                           float sd, double alpha, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  dim3 grid((W + 15) / 16, (H + 7) / 8, njobs);
+  fp_kernel<<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ray_splat(const ProjGeom *d_geom, const SplatJob *d_jobs, int njobs, const int dims[3], int W,
+                             int H, float sd, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  dim3 grid((W + 15) / 16, (H + 7) / 8, njobs);
+  splat_kernel<<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_correction(int n, const float *meas, const float *img, const float *len, float *dual,
+                              double alpha, float *corr, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  correction_kernel<<<(n + 255) / 256, 256, 0, st>>>(n, meas, img, len, dual, alpha, corr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njobs, int maxbox[3], const int dims[3],
+                            int W, int H, double halfW, double halfH, float sdd, double ds, double alpha, float gmax,
+                            int mode, int exact, cudaStream_t st) {
+  if (njobs <= 0 || maxbox[0] <= 0 || maxbox[1] <= 0 || maxbox[2] <= 0) return cudaSuccess;
+  const dim3 block(32, 4, 2);
+  const int zblocks = (maxbox[2] + 1) / 2;
+  const dim3 grid((maxbox[0] + 31) / 32, (maxbox[1] + 3) / 4, zblocks * njobs);
+  const int float_ok = ((double)(float)halfW == halfW && (double)(float)halfH == halfH && (double)(float)ds == ds);
+#define WAP_BP(E, M)                                                                                             \
+  bp_voxel_kernel<E, M><<<grid, block, 0, st>>>(d_geom, d_jobs, zblocks, dims[0], dims[1], W, H, halfW, halfH, sdd, \
+                                                ds, float_ok, alpha, gmax)
+  if (exact) {
+    if (mode == 0) WAP_BP(true, 0);
+    else WAP_BP(true, 1);
+  } else {
+    if (mode == 0) WAP_BP(false, 0);
+    else WAP_BP(false, 1);
+  }
+#undef WAP_BP
+  return cudaGetLastError();
+}
+
+}  // namespace wap
+
+namespace wap {
+namespace {
+__global__ void max_reduce_kernel(const float *__restrict__ d, size_t n, unsigned *out_bits) {
+  // Non-negative-agnostic max via ordered integer keys.
+  float m = -3.4028234663852886e38f;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    m = fmaxf(m, d[i]);
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) {
+    unsigned b = __float_as_uint(m);
+    b = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+    atomicMax(out_bits, b);
+  }
+}
+}  // namespace
+
+cudaError_t launch_max_reduce(const float *d, size_t n, unsigned *d_bits, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(d_bits, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  max_reduce_kernel<<<152, 256, 0, st>>>(d, n, d_bits);
+  return cudaGetLastError();
+}
+
+float decode_max_bits(unsigned b) {
+  b = (b & 0x80000000u) ? (b & 0x7fffffffu) : ~b;
+  float f;
+  memcpy(&f, &b, 4);
+  return f;
+}
+
+}  // namespace wap

@@ -1,0 +1,72 @@
+// Flow-solver and CP-prior kernel interfaces (flow.cu, cp_prior.cu).
+#pragma once
+
+#include <cmath>
+#include <vector>
+
+#include "wap_internal.h"
+
+namespace wap {
+
+struct FlowDims {
+  int n[3];
+  int roi[6];  // margins: x-lo, x-hi, y-lo, y-hi, z-lo, z-hi (optical_flow.h ROI)
+};
+
+struct DericheCoefs {
+  float a0, a1, a2, a3, b1, b2, coefp, coefn;
+  int skip;  // sigma < 0.1: the filter is the identity
+};
+
+// Per-axis resize tables (device pointers).  Shrinking uses taps, growing uses
+// base index + fractional offset accumulated in double as CImg does.
+struct ResizeTables {
+  const int *tap_start = nullptr;  // Sout + 1
+  const int *tap_src = nullptr;
+  const float *tap_w = nullptr;
+  const int *base = nullptr;       // Sout
+  const double *frac = nullptr;    // Sout
+};
+
+DericheCoefs deriche_coefs(float sigma);
+cudaError_t launch_deriche(int axis, const int dims[3], int nc, const DericheCoefs &k, const float *in, float *out,
+                           cudaStream_t st);
+cudaError_t launch_resize_axis(int axis, const int in_dims[3], int nc, int Sout, const ResizeTables &tb,
+                               const float *in, float *out, cudaStream_t st);
+cudaError_t launch_linearize(const FlowDims &D, const float *warp, const float *I1, const float *v, float *u,
+                             float *kx4prev, cudaStream_t st);
+cudaError_t launch_pd_primal(const FlowDims &D, const float *y, const float *u, const float *vcur, float *vnext,
+                             float *kty, int store_kty, int residual, double *acc, cudaStream_t st);
+cudaError_t launch_pd_dual(const FlowDims &D, float *y, const float *u, const float *vnew, const float *vold,
+                           const float *kx4prev, int kxold_mode, float lambda, float sigma1, int residual,
+                           double *acc, cudaStream_t st);
+cudaError_t launch_residual_finish(const double *acc, int nPx, float *err, cudaStream_t st);
+cudaError_t launch_roi_copy(const FlowDims &D, int nch, const float *src, float *dst, cudaStream_t st);
+
+// CP prior (WaP_Tomo.cpp:586-689), batched over frames.
+struct CpArgs {
+  int n[3];
+  int box[6];
+  int f0;          // first frame of the batch
+  int F;           // frames in the batch
+  int Ftot;        // frames in the level (X_bar[Ftot] is the zero volume)
+  float sigma;     // CP_sigma = .9/(L*tau)
+  float tau;       // CP_tau
+  float tv_w, tp_w;
+  float gmax;
+};
+cudaError_t launch_cp_dual(const CpArgs &a, const float *xbar, const float *xbar_zero, float *ytv, float *ytp,
+                           cudaStream_t st);
+cudaError_t launch_cp_primal(const CpArgs &a, const float *ytp, const float *ytv, float *vol, float *xprev,
+                             cudaStream_t st);
+cudaError_t launch_cp_overrelax(const CpArgs &a, const float *vol, const float *xprev, float *xbar, cudaStream_t st);
+
+// Host-side table builders for the resize kernels.
+struct HostResizeAxis {
+  std::vector<int> tap_start, tap_src, base;
+  std::vector<float> tap_w;
+  std::vector<double> frac;
+};
+HostResizeAxis make_resize_axis(int Sin, int Sout);
+
+}  // namespace wap

@@ -1,0 +1,110 @@
+// Shared device/host definitions of the GB300 warp-and-project library.
+//
+// Every translation unit is compiled with -fmad=false: the reference defines
+// its numbers without fused multiply-add, and the parity contract (sample
+// counts and traversal bit-exact, projections and volumes reproducible)
+// depends on each float operation rounding where the reference's does.
+// Kernels that are allowed to differ use explicit __fmaf_rn.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+struct wap_ctx;
+
+namespace wap {
+
+// The stream a context orders its work on (capi.cpp).
+cudaStream_t ctx_stream(wap_ctx *ctx);
+
+// Per-projection geometry, produced on the host by geometry.cpp
+// (TypicalRayProducer.cpp:157-232) and read by the projector kernels.
+struct ProjGeom {
+  float p2m[16];    // pixels -> model (inverse of V2P * Proj * MV)
+  float m2v[16];    // model -> voxel
+  float mvv2m[16];  // MV * V2M: voxel -> camera, used by the voxel-driven BP
+  float eye[4];     // source position in model space
+};
+
+struct ScanDesc;  // forward (wap.h's wap_scan_desc is layout-compatible)
+
+// The reference's min/max macros: ((a) < (b)) ? (a) : (b)
+// (RayCaster.core.h:22-28, WaP_Tomo.cpp:170-176).
+__host__ __device__ __forceinline__ float mac_min(float a, float b) { return (a < b) ? a : b; }
+__host__ __device__ __forceinline__ float mac_max(float a, float b) { return (a > b) ? a : b; }
+__host__ __device__ __forceinline__ int mac_mini(int a, int b) { return (a < b) ? a : b; }
+__host__ __device__ __forceinline__ int mac_maxi(int a, int b) { return (a > b) ? a : b; }
+// std::min / std::max argument order (advection.h, optical_flow.h).
+__host__ __device__ __forceinline__ float std_min(float a, float b) { return (b < a) ? b : a; }
+__host__ __device__ __forceinline__ float std_max(float a, float b) { return (a < b) ? b : a; }
+
+// Column-major 4x4 times vector, summed left to right (Matrix4x4.h).
+__host__ __device__ __forceinline__ void mat4_vec(const float *M, float x, float y, float z, float w, float out[4]) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) out[r] = M[r] * x + M[4 + r] * y + M[8 + r] * z + M[12 + r] * w;
+}
+
+// ---------------------------------------------------------------------------
+// Job descriptors: one kernel launch serves many independent frames.
+// ---------------------------------------------------------------------------
+struct FpJob {
+  const float *vol;   // volume to project
+  int proj;           // projection index (geometry row, measured row)
+  float *img;         // optional: projection (W*H)
+  float *len;         // optional: ray length
+  float *weight;      // optional: sample count
+  const float *meas;  // optional: measured projection -> fused correction
+  float *dual;        // optional: PSART dual row (y = 0 when null)
+  float *corr;        // correction output when meas != null
+};
+
+struct BpJob {
+  float *vol;         // SART: volume updated in place; delta mode: accumulator
+  const float *corr;  // correction image (W*H)
+  int proj;           // geometry row
+  int box[6];         // x0,x1,y0,y1,z0,z1 (half-open)
+};
+
+struct SplatJob {
+  const float *corr;
+  int proj;
+  float *contrib;
+  float *weight;
+};
+
+// Launch helpers (implemented in the .cu files).
+cudaError_t launch_forward(const ProjGeom *d_geom, const FpJob *d_jobs, int njobs, const int dims[3], int W, int H,
+                           float sd, double alpha, cudaStream_t st);
+cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njobs, int maxbox[3], const int dims[3],
+                            int W, int H, double halfW, double halfH, float sdd, double ds, double alpha, float gmax,
+                            int mode, int exact, cudaStream_t st);
+cudaError_t launch_ray_splat(const ProjGeom *d_geom, const SplatJob *d_jobs, int njobs, const int dims[3], int W,
+                             int H, float sd, cudaStream_t st);
+cudaError_t launch_correction(int n, const float *meas, const float *img, const float *len, float *dual,
+                              double alpha, float *corr, cudaStream_t st);
+
+struct AdvectJob {
+  const float *vel;  // 3 planar channels
+  const float *src;  // nc planar channels
+  float *out;        // nc planar channels
+  float dt;
+};
+// Cell-centre world coordinates per axis (advection.h:24-29), sum(dims) floats.
+void world_table(const int dims[3], const float aabb[6], float *h);
+cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d_world, const AdvectJob *d_jobs,
+                          int njobs, int nc, cudaStream_t st);
+// vol = clamp_cut(vol + alpha*adv) then max(vol*roi, 0) (WaP_Tomo.cpp:1378-1412).
+cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st);
+cudaError_t launch_roi_floor(size_t n, float *vol, cudaStream_t st);
+struct AccJob {
+  float *vol;
+  const float *adv;
+};
+cudaError_t launch_wap_accumulate_batch(const AccJob *d_jobs, int njobs, size_t n, double alpha, float gmax,
+                                        cudaStream_t st);
+cudaError_t launch_max_reduce(const float *d, size_t n, unsigned *d_bits, cudaStream_t st);
+float decode_max_bits(unsigned b);
+
+}  // namespace wap
