@@ -31,7 +31,8 @@ enum {
   WAP_ENOMEM = 2,   /* device allocation failed */
   WAP_ECUDA = 3,    /* CUDA runtime error */
   WAP_ESTATE = 4,   /* call out of order (e.g. no level set up) */
-  WAP_ENODEV = 5    /* no usable GPU */
+  WAP_ENODEV = 5,   /* no usable GPU */
+  WAP_ETOOBIG = 6   /* problem larger than a fixed-capacity entry point allows */
 };
 
 typedef struct wap_ctx wap_ctx;
@@ -225,6 +226,26 @@ WAP_API int wap_projection_geometry(const wap_scan_desc *scan, double angle_deg,
 WAP_API int wap_cg_screened_laplacian(wap_ctx *ctx, const int *dims, float a, float b, const float *d_rhs,
                                       float *d_x, float rel_tol, int max_iters, float abs_tol, int mode,
                                       int *h_iters);
+
+/* Allocation-free variant of wap_cg_screened_laplacian.  This entry point has
+ * no counterpart in the reference.  It exists for callers that cannot have the
+ * library allocate device memory: applications whose memory pool has reserved
+ * the device, where an extra cudaMalloc fails, and serving loops that cannot
+ * absorb the device-wide synchronisation of cudaFree.  Its scratch (the CG
+ * vectors r, p, Ap plus FP64 accumulators) lives in one fixed device array of
+ * 3 * WAP_CG_NOALLOC_MAX_VOXELS floats (3 MiB) + 256 bytes, which every GPU
+ * that loads the library holds until the process exits.  Grids with more than
+ * WAP_CG_NOALLOC_MAX_VOXELS voxels return WAP_ETOOBIG.  It needs no context:
+ * it works on the current device and orders its work on cuda_stream (NULL =
+ * the legacy default stream), with the same arguments and results as
+ * wap_cg_screened_laplacian.  The first call on each device looks the scratch
+ * address up (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  Every call reuses the same scratch, so
+ * calls that overlap on the GPU (other streams, other host threads) race. */
+#define WAP_CG_NOALLOC_MAX_VOXELS 262144
+WAP_API int wap_cg_screened_laplacian_noalloc(void *cuda_stream, const int *dims, float a, float b,
+                                              const float *d_rhs, float *d_x, float rel_tol, int max_iters,
+                                              float abs_tol, int mode, int *h_iters);
 
 #ifdef __cplusplus
 }

@@ -163,3 +163,94 @@ done:
   if (h_iters) *h_iters = iters;
   return status;
 }
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of wap_cg_screened_laplacian.
+//
+// Some callers cannot let a library allocate device memory on their behalf:
+// an application whose memory pool has already reserved the device (an extra
+// cudaMalloc then fails with out-of-memory), or a serving loop that keeps
+// other streams busy and cannot absorb the device-wide synchronisation that
+// cudaFree implies.  This entry point keeps its work vectors (r, p, Ap), its
+// FP64 dot-product accumulators and its scalars in one fixed array below,
+// which every GPU that loads the library holds until the process exits.
+// ---------------------------------------------------------------------------
+#include <mutex>
+
+namespace wap {
+namespace {
+
+constexpr size_t kNoAllocVecBytes = sizeof(float) * 3 * (size_t)WAP_CG_NOALLOC_MAX_VOXELS;
+constexpr size_t kNoAllocBytes = kNoAllocVecBytes + 256;  // + 4 doubles, 4 floats, padding
+
+// The scratch every call shares: r, p, Ap, then the accumulators and scalars.
+static __device__ __align__(256) unsigned char g_cg_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the scratch, looked up once per device (host code cannot
+// use the symbol itself: on the host it names a stand-in, not device memory).
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[128] = {nullptr};
+
+int noalloc_scratch(void **out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return WAP_ENODEV;
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_cg_noalloc_scratch) != cudaSuccess || !p) return WAP_ECUDA;
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return WAP_OK;
+}
+
+}  // namespace
+}  // namespace wap
+
+extern "C" int wap_cg_screened_laplacian_noalloc(void *cuda_stream, const int *dims, float a, float b,
+                                                 const float *d_rhs, float *d_x, float rel_tol, int max_iters,
+                                                 float abs_tol, int mode, int *h_iters) {
+  if (!dims || !d_rhs || !d_x || dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || max_iters < 0) return WAP_EINVAL;
+  const size_t n = (size_t)dims[0] * dims[1] * dims[2];
+  if (n > (size_t)WAP_CG_NOALLOC_MAX_VOXELS) return WAP_ETOOBIG;
+  void *base = nullptr;
+  int rc = noalloc_scratch(&base);
+  if (rc != WAP_OK) return rc;
+  cudaStream_t st = (cudaStream_t)cuda_stream;
+  unsigned char *bytes = (unsigned char *)base;
+  float *r = (float *)bytes, *p = r + n, *ap = r + 2 * n;
+  double *acc = (double *)(bytes + kNoAllocVecBytes);
+  float *scal = (float *)(bytes + kNoAllocVecBytes + 4 * sizeof(double));
+  const Lap L{dims[0], dims[1], dims[2], a, b};
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  int iters = 0;
+  float h[4];
+  // The accumulators keep the previous call's sums: clear them before use.
+  if (cudaMemsetAsync(acc, 0, sizeof(double) * 4, st) != cudaSuccess) return WAP_ECUDA;
+  lap_apply_kernel<<<blocks, 256, 0, st>>>(L, d_x, ap, nullptr);
+  cg_init_kernel<<<blocks, 256, 0, st>>>(n, d_rhs, ap, r, p, acc);
+  cg_store_rr_kernel<<<1, 1, 0, st>>>(acc, scal, 0);
+  if (cudaMemcpyAsync(h, scal, sizeof(float), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return WAP_ECUDA;
+  const float rr_init = h[0];
+  if (!(std::sqrt(rr_init) < abs_tol)) {
+    for (int it = 0; it < max_iters; ++it) {
+      iters = it + 1;
+      cudaMemsetAsync(acc, 0, sizeof(double) * 2, st);
+      lap_apply_kernel<<<blocks, 256, 0, st>>>(L, p, ap, acc);
+      cg_alpha_kernel<<<1, 1, 0, st>>>(acc, scal);
+      cg_update_kernel<<<blocks, 256, 0, st>>>(n, scal, p, ap, d_x, r, acc + 1);
+      cg_store_rr_kernel<<<1, 1, 0, st>>>(acc + 1, scal, 2);
+      if (cudaMemcpyAsync(h, scal, sizeof(float) * 3, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+        return WAP_ECUDA;
+      if (std::sqrt(h[2] / rr_init) < rel_tol) break;
+      cg_direction_kernel<<<blocks, 256, 0, st>>>(n, scal, r, p, mode);
+      cg_shift_rr_kernel<<<1, 1, 0, st>>>(scal);
+    }
+  }
+  if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return WAP_ECUDA;
+  if (h_iters) *h_iters = iters;
+  return WAP_OK;
+}
