@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -61,7 +62,7 @@ struct Status {
 // Flow-solver workspace for one grid size (reused across pairs and calls).
 struct FlowWork {
   int n[3] = {0, 0, 0};
-  DevMem va, vb, y, u, kty, kx4prev, warp, acc, err, world;
+  DevMem va, vb, y, y2, u, kty, kx4prev, warp, acc, err, world;
   float aabb_key[6] = {0, 0, 0, 0, 0, 0};
 };
 
@@ -110,6 +111,7 @@ struct wap_ctx {
 
   wap_stats stats{};
   int profiling = 0;
+  std::map<uint32_t, int> fastdiv_ok;  // shrink divisor bits -> exhaustively verified
   std::vector<cudaEvent_t> pd_events;  // pairs, reused per 50-iteration chunk
   std::string err;
 };
@@ -409,7 +411,8 @@ FlowWork *flow_work(wap_ctx *ctx, const int dims[3]) {
   const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
   for (int a = 0; a < 3; ++a) w->n[a] = dims[a];
   if (w->va.ensure(sizeof(float) * 3 * nv) || w->vb.ensure(sizeof(float) * 3 * nv) ||
-      w->y.ensure(sizeof(float) * 10 * nv) || w->u.ensure(sizeof(float) * 4 * nv) ||
+      w->y.ensure(sizeof(float) * 10 * nv) || w->y2.ensure(sizeof(float) * 10 * nv) ||
+      w->u.ensure(sizeof(float) * 4 * nv) ||
       w->kty.ensure(sizeof(float) * 3 * nv) || w->kx4prev.ensure(sizeof(float) * nv) ||
       w->warp.ensure(sizeof(float) * nv) || w->acc.ensure(sizeof(double) * 2) || w->err.ensure(sizeof(float)) ||
       w->world.ensure(sizeof(float) * (dims[0] + dims[1] + dims[2])))
@@ -441,6 +444,10 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   }
   float *vcur = w->va.as<float>(), *vnext = w->vb.as<float>();
   float *y = w->y.as<float>();
+  float *ycur = y, *ynext = w->y2.as<float>();
+  // z-chunk per block: at least ~4 waves of 2 resident blocks over 152 SMs.
+  const int tiles = ((dims[0] + 31) / 32) * ((dims[1] + 6) / 7);
+  const int zchunk = std::max(2, std::min(64, dims[2] * tiles / 1216));
   CU(cudaMemcpyAsync(vcur, V, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
   CU(cudaMemcpyAsync(vnext, V, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
   for (int q = 0; q < 3; ++q)
@@ -450,6 +457,24 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   CU(cudaMemsetAsync(w->kty.p, 0, sizeof(float) * 3 * nv, ctx->stream));
   const float sigma1 = std::min(1.0f / 3.0f, std::min(1.0f / 3.0f, 1.0f / 3.0f));
   double *acc = w->acc.as<double>();
+  // The dual's shrink divides by the constant lambda + 2 sigma1; the FMA-
+  // corrected reciprocal is used only once it is proven bit-identical to IEEE
+  // division for this constant over all 2^32 inputs.
+  const float den = lambda + 2 * sigma1;
+  const float rinv = 1.0f / den;
+  uint32_t den_bits;
+  std::memcpy(&den_bits, &den, 4);
+  auto fd = ctx->fastdiv_ok.find(den_bits);
+  if (fd == ctx->fastdiv_ok.end()) {
+    DevMem bad;
+    CU(bad.ensure(sizeof(unsigned long long)));
+    KL(launch_pd_fastdiv_check(den, rinv, bad.as<unsigned long long>(), ctx->stream));
+    unsigned long long nbad = 1;
+    CU(cudaMemcpyAsync(&nbad, bad.p, sizeof(nbad), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    fd = ctx->fastdiv_ok.emplace(den_bits, nbad == 0 ? 1 : 0).first;
+  }
+  const int fastdiv = fd->second;
   AdvectJob aj{vcur, I2, w->warp.as<float>(), -1.0f};
   for (int wi = 0; wi < nwarps; ++wi) {
     // advect I2 by the current flow, dt = -1 (optical_flow.h:418)
@@ -485,12 +510,12 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
       const int store = ((it + 1) % 50 == 0);
       if (res) CU(cudaMemsetAsync(acc, 0, sizeof(double) * 2, ctx->stream));
       if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending], ctx->stream));
-      KL(launch_pd_primal(D, y, w->u.as<float>(), vcur, vnext, w->kty.as<float>(), store, res, acc, ctx->stream));
       const int mode = (it == 1) ? (wi == 0 ? 1 : 2) : 0;
-      KL(launch_pd_dual(D, y, w->u.as<float>(), vnext, vcur, w->kx4prev.as<float>(), mode, lambda, sigma1, res,
-                        acc + 1, ctx->stream));
+      KL(launch_pd_fused(D, zchunk, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
+                         w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, store, res, acc, ctx->stream));
       if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending++ + 1], ctx->stream));
       std::swap(vcur, vnext);
+      std::swap(ycur, ynext);
       if (res) {
         KL(launch_residual_finish(acc, (int)nv, w->err.as<float>(), ctx->stream));
         CU(cudaMemcpyAsync(&err, w->err.p, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
@@ -508,8 +533,8 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     ctx->stats.flow_pd_iterations += it;
   }
   CU(cudaMemcpyAsync(V, vcur, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
-  for (int q = 0; q < 3; ++q) KL(launch_roi_copy(D, 3, y + 3 * q * nv, Y[q], ctx->stream));
-  KL(launch_roi_copy(D, 1, y + 9 * nv, Y[3], ctx->stream));
+  for (int q = 0; q < 3; ++q) KL(launch_roi_copy(D, 3, ycur + 3 * q * nv, Y[q], ctx->stream));
+  KL(launch_roi_copy(D, 1, ycur + 9 * nv, Y[3], ctx->stream));
   return WAP_OK;
 }
 

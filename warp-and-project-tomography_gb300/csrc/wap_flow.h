@@ -35,11 +35,13 @@ cudaError_t launch_resize_axis(int axis, const int in_dims[3], int nc, int Sout,
                                const float *in, float *out, cudaStream_t st);
 cudaError_t launch_linearize(const FlowDims &D, const float *warp, const float *I1, const float *v, float *u,
                              float *kx4prev, cudaStream_t st);
-cudaError_t launch_pd_primal(const FlowDims &D, const float *y, const float *u, const float *vcur, float *vnext,
-                             float *kty, int store_kty, int residual, double *acc, cudaStream_t st);
-cudaError_t launch_pd_dual(const FlowDims &D, float *y, const float *u, const float *vnew, const float *vold,
-                           const float *kx4prev, int kxold_mode, float lambda, float sigma1, int residual,
-                           double *acc, cudaStream_t st);
+cudaError_t launch_pd_fused(const FlowDims &D, int zchunk, const float *yin, float *yout, const float *u,
+                            const float *vin, float *vout, float *kty, const float *kx4prev, int kxold_mode,
+                            float lambda, float sigma1, float rinv, int fastdiv, int store_kty, int residual,
+                            double *acc, cudaStream_t st);
+// Counts the float inputs for which the FMA-corrected division by den differs
+// from IEEE division (0 proves the fast path exact for this den).
+cudaError_t launch_pd_fastdiv_check(float den, float rinv, unsigned long long *d_bad, cudaStream_t st);
 cudaError_t launch_residual_finish(const double *acc, int nPx, float *err, cudaStream_t st);
 cudaError_t launch_roi_copy(const FlowDims &D, int nch, const float *src, float *dst, cudaStream_t st);
 
