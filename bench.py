@@ -227,6 +227,7 @@ def run_gb300(args):
     import torch
     import wap
     import build
+    import replicas
     rank, world, local, dist = dist_init(args)
     torch.cuda.set_device(local)
     build.build()
@@ -265,8 +266,7 @@ def run_gb300(args):
         ctx.call("wap_frame_volume_download", f, h_vol.data_ptr())
         ctx.call("wap_frame_flow_download", f, h_flow.data_ptr())
 
-    frames = list(range(F - 1))
-    order = [frames[(rank * 7 + i) % len(frames)] for i in range(args.warmup + args.steps)]
+    order = replicas.frame_order(rank, args.warmup + args.steps, F)
     for i in range(args.warmup):
         f = order[i]
         with torch.cuda.stream(stream):
@@ -308,13 +308,11 @@ def run_gb300(args):
     clk = clocks.stop()
     if dist:
         import torch.distributed as tdist
-        tt = torch.tensor([t_dev, t_e2e], dtype=torch.float64, device="cuda")
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        t_dev, t_e2e = float(tt[0]), float(tt[1])
+        t_dev, t_e2e = replicas.max_over_ranks([t_dev, t_e2e], tdist, device="cuda")
         tdist.barrier()
     K = args.steps
-    value = world * (K / F) / t_dev
-    e2e = world * (K / F) / t_e2e
+    value = replicas.aggregate_rate(world, K / F, t_dev)
+    e2e = replicas.aggregate_rate(world, K / F, t_e2e)
     pd_ms = agg["ms_pd"] / max(agg["pd_timed"], 1)
     achieved = PD_BYTES_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
