@@ -128,6 +128,7 @@ class Oracle:
         _bind(L, "orc_gradient", None, [_i32, _f32, _f32, _f32, _f32])
         _bind(L, "orc_flow_level", _c_int, [_i32, _f32, _f32, _f32, _f32, _f32, _f32, _f32, _c_float, _c_float,
                                             _c_int, _c_int, _f32, _i32, _c_int, _i32])
+        _bind(L, "orc_last_pd_seconds", _c_double, [])
         _bind(L, "orc_flow_multiscale", _c_int, [_i32, _f32, _f32, _f32, _c_float, _c_float, _c_int, _c_int,
                                                  _c_float, _c_float, _c_int, _i32, _c_int, _f32])
         _bind(L, "orc_sart_prox", None, [S, _f64, _f32, _c_int, _c_int, _c_int, _i32, _f32, _f32])

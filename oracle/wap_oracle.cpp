@@ -799,7 +799,11 @@ inline float my_abs(float x) { return x > 0 ? x : -x; }
 
 }  // namespace
 
+static double g_last_pd_seconds = 0.0;
+
 extern "C" {
+
+double orc_last_pd_seconds() { return g_last_pd_seconds; }
 
 int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V, float *Y1, float *Y2, float *Y3,
                    float *Y4, float tol, float lambda, int max_iters, int nwarps, const float aabb[6],
@@ -831,6 +835,7 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
   const int x0 = roi[0], x1 = dims[0] - roi[1], y0 = roi[2], y1 = dims[1] - roi[3], z0 = roi[4], z1 = dims[2] - roi[5];
   float p = 0.0f, d = 0.0f;
   int total = 0;
+  double pd_seconds = 0.0;
   std::vector<float> Vimg(3 * n), warp(n), gx(n), gy(n), gz(n);
   for (int w = 0; w < nwarps; ++w) {
     // _inputV holds v inside the ROI (written by the primal) and the input outside.
@@ -861,6 +866,7 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
     int it = 0;
     float err = 1.0f;
     const float *uu[3] = {ux.data(), uy.data(), uz.data()};
+    const double t_pd = omp_get_wtime();
     while (err > tol && it <= max_iters) {
       ++it;
       const bool res = (it % 50 == 0);
@@ -941,9 +947,11 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
       }
       if (res) err = (d * d + p * p) / (float)nPx;
     }
+    pd_seconds += omp_get_wtime() - t_pd;
     if (iters_out) iters_out[w] = it;
     total += it;
   }
+  g_last_pd_seconds = pd_seconds;
   // write back (optical_flow.h:840-877): ROI only
   for (int k = z0; k < z1; ++k)
     for (int j = y0; j < y1; ++j)

@@ -31,7 +31,7 @@ typedef struct {
   double alpha;     /* -a: SART relaxation */
   double tv_w;      /* -s: TV weight */
   double tp_w;      /* -t: temporal weight */
-  float gmax;       /* max of the projection stack (WaP_Tomo.cpp:347-348) */
+  float gmax;       /* G_Max: max of the first projection image (WaP_Tomo.cpp:347-348) */
   int threads;      /* OpenMP threads, 0 = runtime default */
 } orc_scan;
 
@@ -89,6 +89,9 @@ void orc_gradient(const int dims[3], const float *src, float *gx, float *gy, flo
 int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V, float *Y1, float *Y2, float *Y3,
                    float *Y4, float tol, float lambda, int max_iters, int nwarps, const float aabb[6],
                    const int roi6[6], int deterministic, int *iters_out);
+
+/* Wall time of the primal-dual loops of the last orc_flow_level call. */
+double orc_last_pd_seconds(void);
 
 /* Coarse-to-fine wrapper (optical_flow.h:1002-1126) as Render calls it. */
 int orc_flow_multiscale(const int dims[3], const float *I1, const float *I2, const float *V0, float tol,
