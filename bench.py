@@ -48,6 +48,9 @@ PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
 # 10 dual components (y1..y3, y4) and the 3 flow components, read the
 # 4-component linearisation (ux, uy, uz, ut); tau and sigma2 derive from u.
 PD_BYTES_PER_VOXEL = 4 * (10 + 10 + 3 + 3 + 4)
+# DRAM bytes (read + write) of one primal-dual launch at 256^3, from an ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of kernel_bench.py.
+PD_TRAFFIC_256 = 1.98e9
 
 
 def parse():
@@ -326,10 +329,11 @@ def run_gb300(args):
         "e2e": {"value": e2e, "unit": "outer-iter/s", "h2d_bytes_per_step": h2d_bytes // K,
                 "d2h_bytes_per_step": 4 * nv * 4},
         "gpu_launches": int(agg["kernel_launches"]),
-        "roofline": {"kernel": "flow primal-dual iteration (pd_primal + pd_dual) at 256^3", "bound": "hbm",
+        "roofline": {"kernel": "pd_fused_kernel (one flow primal-dual iteration) at %d^3" % n, "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": None, "bytes_per_voxel": PD_BYTES_PER_VOXEL,
-                     "ms_per_launch": pd_ms},
+                     "peak_source": peak_kind, "traffic": PD_TRAFFIC_256 if n == 256 else None,
+                     "algorithmic_bytes": PD_BYTES_PER_VOXEL * pd_vox, "bytes_per_voxel": PD_BYTES_PER_VOXEL,
+                     "ms_per_launch": pd_ms, "launches_timed": int(agg["pd_timed"])},
         "phase_ms_per_step": {"cp_sart": agg["ms_cp"] / K, "flow": agg["ms_flow"] / K, "wap": agg["ms_wap"] / K},
         "pd_iterations_per_step": agg["flow_pd_iterations"] / K,
         "op_counts_per_outer_iteration": {k: agg[k] * F / K for k in ("projections", "backprojections",
