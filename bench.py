@@ -44,13 +44,18 @@ for _p in (PKG, os.path.join(REPO, "tests"), os.path.join(REPO, "oracle")):
 
 METRIC = "WaP outer-iter/s at 256^3 x 192 proj"
 PEAKS = os.path.join(REPO, "MEASURED_PEAKS.json")
-# Compulsory bytes of one primal-dual iteration per voxel: read and write the
-# 10 dual components (y1..y3, y4) and the 3 flow components, read the
-# 4-component linearisation (ux, uy, uz, ut); tau and sigma2 derive from u.
-PD_BYTES_PER_VOXEL = 4 * (10 + 10 + 3 + 3 + 4)
-# DRAM bytes (read + write) of one primal-dual launch at 256^3, from an ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum) of kernel_bench.py.
-PD_TRAFFIC_256 = 1.98e9
+# Algorithmic bytes of one primal-dual iteration per voxel, the figure the
+# roofline is quoted against: the two-kernel minimum of the iteration (30
+# y-words, 15 v-words, 7 u-words; optical_flow.h:478-813).
+PD_BYTES_PER_VOXEL = 4 * (30 + 15 + 7)
+# The single-pass minimum (read and write y and v once, read u once), which
+# only the fused kernel form reaches.
+PD_BYTES_MIN_PER_VOXEL = 4 * (10 + 10 + 3 + 3 + 4)
+# DRAM bytes (read + write) of one primal-dual iteration at 256^3 per kernel
+# form (1 fused, 2 primal + dual), from ncu captures (dram__bytes_read.sum +
+# dram__bytes_write.sum) of kernel_bench.py.
+PD_TRAFFIC_256 = {1: 1.98e9, 2: None}
+PD_FORMS = {1: "pd_fused_kernel", 2: "pd_primal_kernel + pd_dual_kernel"}
 
 
 def parse():
@@ -316,6 +321,8 @@ def run_gb300(args):
     pd_ms = agg["ms_pd"] / max(agg["pd_timed"], 1)
     achieved = PD_BYTES_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    pd_side = round(pd_vox ** (1.0 / 3.0))
+    form, zchunk = ctx.get_tuning([pd_side] * 3)
     result = {
         "metric": METRIC, "value": value, "unit": "outer-iter/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": t_dev / K * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -329,10 +336,14 @@ def run_gb300(args):
         "e2e": {"value": e2e, "unit": "outer-iter/s", "h2d_bytes_per_step": h2d_bytes // K,
                 "d2h_bytes_per_step": 4 * nv * 4},
         "gpu_launches": int(agg["kernel_launches"]),
-        "roofline": {"kernel": "pd_fused_kernel (one flow primal-dual iteration) at %d^3" % n, "bound": "hbm",
+        "roofline": {"kernel": "one flow primal-dual iteration at %d^3: %s (z-chunk %d, autotuned)"
+                               % (pd_side, PD_FORMS.get(form, "?"), zchunk), "bound": "hbm",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": PD_TRAFFIC_256 if n == 256 else None,
+                     "peak_source": peak_kind,
+                     "traffic": PD_TRAFFIC_256.get(form) if pd_side == 256 else None,
                      "algorithmic_bytes": PD_BYTES_PER_VOXEL * pd_vox, "bytes_per_voxel": PD_BYTES_PER_VOXEL,
+                     "min_bytes_per_voxel": PD_BYTES_MIN_PER_VOXEL,
+                     "frac_at_min_bytes": PD_BYTES_MIN_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9 / peak,
                      "ms_per_launch": pd_ms, "launches_timed": int(agg["pd_timed"])},
         "phase_ms_per_step": {"cp_sart": agg["ms_cp"] / K, "flow": agg["ms_flow"] / K, "wap": agg["ms_wap"] / K},
         "pd_iterations_per_step": agg["flow_pd_iterations"] / K,

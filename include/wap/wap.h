@@ -103,6 +103,52 @@ WAP_API int wap_get_stats(wap_ctx *ctx, wap_stats *out);
  * the context's stream (wap_stats.ms_pd); 0 (default): no per-launch events. */
 WAP_API int wap_set_profiling(wap_ctx *ctx, int on);
 
+/* A context without a scan, for the calls that take their grid as arguments
+ * (wap_advect, wap_blur, wap_resize, wap_flow_level, wap_flow_multiscale,
+ * wap_cg_screened_laplacian and the memory helpers below);
+ * the scan-dependent calls return WAP_ESTATE on it. */
+WAP_API int wap_create_compute(wap_ctx **out, int device);
+
+/* Device memory helpers, so that callers need no CUDA headers: allocation on
+ * the context's device, and copies ordered on the context's stream that
+ * return when the copy is complete. */
+WAP_API int wap_alloc(wap_ctx *ctx, size_t bytes, void **d_out);
+WAP_API int wap_free(wap_ctx *ctx, void *d_ptr);
+WAP_API int wap_copy_to_device(wap_ctx *ctx, void *d_dst, const void *h_src, size_t bytes);
+WAP_API int wap_copy_to_host(wap_ctx *ctx, void *h_dst, const void *d_src, size_t bytes);
+WAP_API int wap_fill_zero(wap_ctx *ctx, void *d_ptr, size_t bytes);
+
+/* Observer of the solver's intermediate states, the points at which the
+ * reference writes its Analyze dumps:
+ *   WAP_EV_SART  after the SART proximal operator of frame a in CP iteration b
+ *                (b = 1..n_cp), d_data = the frame's volume
+ *                (WaP_Tomo.cpp:1669);
+ *   WAP_EV_FLOW  after the flow of the pair (a, a+1), d_data = frame a's
+ *                3-channel flow (WaP_Tomo.cpp:764-771);
+ *   WAP_EV_WARP  after the warp-and-project step of frame a at projection b,
+ *                d_data = the frame's volume (WaP_Tomo.cpp:1417-1418).
+ * The call comes from the thread running the outer iteration, after the
+ * context's stream has finished the step; d_data is valid only during the
+ * call.  The observer may use the device-pointer calls and the memory helpers
+ * on the same context (e.g. wap_advect, wap_copy_to_host) but not the solver
+ * calls (wap_sart_prox, wap_warp_and_project, wap_outer_iteration*).  Frames
+ * that the library batches into one launch report one event each, in frame
+ * order, after that launch; each event's data is the state the reference
+ * dumps at that point.  Results are identical with or without an observer.
+ * fn = NULL removes it. */
+enum { WAP_EV_SART = 1, WAP_EV_FLOW = 2, WAP_EV_WARP = 3 };
+typedef void (*wap_observer_fn)(void *user, int event, int level, int a, int b, const float *d_data);
+WAP_API int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user);
+
+/* Kernel-shape choices (results are identical for every choice; only speed
+ * changes).  key "pd_form": 0 = autotuned per grid size (default), 1 = the
+ * fused primal-dual kernel, 2 = the primal + dual kernel pair; "pd_zchunk":
+ * z planes per block, 0 = autotuned / default.  Unknown keys are WAP_EINVAL. */
+WAP_API int wap_set_tuning(wap_ctx *ctx, const char *key, int value);
+/* The form and z-chunk used for a grid (after its first flow level; before
+ * that, the forced values or 0). */
+WAP_API int wap_get_tuning(wap_ctx *ctx, const int *dims, int *h_form, int *h_zchunk);
+
 /* Projection stack W*H*nproj (PSART ctor loading + get_split, WaP_Tomo.cpp:339);
  * also sets G_Max = max of the first projection image, projslevel[0][0]
  * (WaP_Tomo.cpp:347-348). */

@@ -238,6 +238,33 @@ class Oracle:
                                                   abs_tol, mode)
 
 
+def lds_angles(np_, ns, p, nz):
+    """Low-discrepancy scanning angles, a line-by-line restatement of
+    Sampling_Model/low discrepancy sequence/Low_discrepency_squence.m:15-45
+    (van der Corput radical inverse in base p over Ns circle segments, a
+    0-degree projection before every Nz-th), in IEEE double like MATLAB."""
+    seq = []
+    i = 0
+    while len(seq) < np_:
+        if len(seq) > 0 and len(seq) % nz == 0:
+            seq.append(0.0)
+        b = i
+        i += 1
+        r = 0.0
+        q = 1.0 / p
+        while b != 0:
+            a = b % p
+            r = r + a * q
+            q = q / p
+            b = b // p
+        r = 360 * r / ns
+        k = 0
+        while len(seq) < np_ and k < ns:
+            seq.append(r + k * 360 / ns)
+            k += 1
+    return np.array(seq[:np_] if len(seq) > np_ else seq, np.float64)
+
+
 class Reference:
     """The reference's own code (``_ref/libwapref.so``); one PSART session."""
 
@@ -271,6 +298,9 @@ class Reference:
                                                   _c_float, _c_float, _c_int, _i32, _f32])
         _bind(L, "wref_cg_screened_laplacian", _c_int, [_i32, _c_float, _c_float, _f32, _f32, _c_float, _c_int,
                                                         _c_float])
+        _bind(L, "wref_save_analyze", _c_int, [ctypes.c_char_p, _f32, _i32])
+        _bind(L, "wref_load_analyze", _c_int, [ctypes.c_char_p, _f32, ctypes.c_longlong, _i32])
+        _bind(L, "wref_split_z", _c_int, [_c_int, _c_int, _i32, _i32])
 
     def create(self, scan, projs, angles, workdir):
         r = self.lib.wref_create(scan.vol[0], scan.vol[1], scan.vol[2], scan.det[0], scan.det[1], scan.nproj,

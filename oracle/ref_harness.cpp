@@ -458,3 +458,54 @@ int wref_cg_screened_laplacian(const int *dims, float a, float b, const float *r
   return 0;
 }
 }
+
+extern "C" {
+// CImg<float>::save_analyze (CImg.h:51715-51790), the writer of every
+// reference output volume.
+int wref_save_analyze(const char *path, const float *data, const int *dims4) {
+  image I(dims4[0], dims4[1], dims4[2], dims4[3]);
+  std::memcpy(I.data(), data, I.size() * 4);
+  try {
+    I.save_analyze(path);
+  } catch (...) {
+    return -1;
+  }
+  return 0;
+}
+
+// CImg<float> load of an Analyze/NIfTI file (CImg.h:47829-47955), the loader
+// behind PSART's `image(pInput[0])` (WaP_Tomo.cpp:339).  dims4 gets W,H,D,C.
+int wref_load_analyze(const char *path, float *out, long long cap, int *dims4) {
+  image I;
+  try {
+    I.load_analyze(path);
+  } catch (...) {
+    return -1;
+  }
+  dims4[0] = I.width();
+  dims4[1] = I.height();
+  dims4[2] = I.depth();
+  dims4[3] = I.spectrum();
+  if ((long long)I.size() > cap) return -2;
+  std::memcpy(out, I.data(), I.size() * 4);
+  return 0;
+}
+
+// CImg::get_split('z', nb) on a 1x1xdepth ramp: first slice and slice count
+// of each piece (CImg.h:31389-31431).
+int wref_split_z(int depth, int nb, int *first, int *count) {
+  image I(1, 1, depth, 1);
+  for (int k = 0; k < depth; ++k) I(0, 0, k) = (float)k;
+  imagelist L;
+  try {
+    L = I.get_split('z', nb);
+  } catch (...) {
+    return -1;
+  }
+  for (int k = 0; k < (int)L.size(); ++k) {
+    first[k] = (int)L[k](0, 0, 0);
+    count[k] = L[k].depth();
+  }
+  return (int)L.size();
+}
+}

@@ -8,6 +8,7 @@ Single-threaded (OMP_NUM_THREADS=1) so the flow residual sums run in loop
 order.
 
     OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+    python tests/golden/make_golden.py formats     # file formats only
 """
 import os
 import sys
@@ -124,7 +125,79 @@ def render(ref, orc):
     ref.lib.wref_destroy()
 
 
+def _analyze_header(dims4, datatype, bitpix, scale, vox_offset, big_endian, hsize=348):
+    import struct
+    e = ">" if big_endian else "<"
+    h = bytearray(hsize)
+    struct.pack_into(e + "i", h, 0, 348)
+    struct.pack_into(e + "5h", h, 40, 4, *dims4)
+    struct.pack_into(e + "h", h, 70, datatype)
+    struct.pack_into(e + "h", h, 72, bitpix)
+    struct.pack_into(e + "4f", h, 76, 0.0, 1.0, 1.0, 1.0)
+    struct.pack_into(e + "f", h, 108, vox_offset)
+    struct.pack_into(e + "f", h, 112, scale)
+    return bytes(h)
+
+
+def formats(ref):
+    """Analyze/NIfTI files as CImg loads and saves them, and CImg's z-split."""
+    rng = np.random.default_rng(40)
+    dims4 = (5, 4, 3, 2)
+    n = int(np.prod(dims4))
+    cases = [  # name, numpy type, Analyze code, scale, big endian, single file
+        ("f32_le", np.float32, 16, 0.5, False, False),
+        ("i16_be", np.int16, 4, 0.0, True, False),
+        ("u8_le", np.uint8, 2, 2.0, False, False),
+        ("i32_le", np.int32, 8, 1.0, False, False),
+        ("f64_nii", np.float64, 64, 1.0, False, True),
+        ("f32_be_nii", np.float32, 16, 1.0, True, True),
+    ]
+    out = {}
+    tmp = tempfile.mkdtemp()
+    for name, dt, code, scale, be, single in cases:
+        if np.issubdtype(dt, np.integer):
+            info = np.iinfo(dt)
+            data = rng.integers(max(info.min, -3000), min(info.max, 3000), size=n).astype(dt)
+        else:
+            data = (rng.normal(size=n) * 10).astype(dt)
+        raw = data.astype(np.dtype(dt).newbyteorder(">" if be else "<")).tobytes()
+        if single:
+            hdr = _analyze_header(dims4, code, np.dtype(dt).itemsize, scale, 352.0, be, hsize=352)
+            path = os.path.join(tmp, name + ".nii")
+            open(path, "wb").write(hdr + raw)
+        else:
+            hdr = _analyze_header(dims4, code, np.dtype(dt).itemsize, scale, 0.0, be)
+            path = os.path.join(tmp, name + ".hdr")
+            open(path, "wb").write(hdr)
+            open(os.path.join(tmp, name + ".img"), "wb").write(raw)
+        got = np.zeros(n, np.float32)
+        d = np.zeros(4, np.int32)
+        assert ref.lib.wref_load_analyze(path.encode(), got, n, d) == 0, name
+        assert tuple(d) == dims4
+        out[name + "_hdr"] = np.frombuffer(hdr, np.uint8)
+        out[name + "_raw"] = np.frombuffer(raw, np.uint8)
+        out[name + "_loaded"] = got
+    img = (rng.normal(size=dims4[::-1]) * 3).astype(np.float32)
+    path = os.path.join(tmp, "saved.hdr")
+    assert ref.lib.wref_save_analyze(path.encode(), img, np.array(dims4, np.int32)) == 0
+    out["save_data"] = img
+    out["save_hdr"] = np.frombuffer(open(path, "rb").read(), np.uint8)
+    out["save_img"] = np.frombuffer(open(os.path.join(tmp, "saved.img"), "rb").read(), np.uint8)
+    splits = [(192, 192), (200, 192), (7, 3), (10, 4), (33, 5), (5, 5), (9, 1), (384, 192), (191, 64)]
+    table = []
+    for depth, nb in splits:
+        first = np.zeros(nb, np.int32)
+        count = np.zeros(nb, np.int32)
+        assert ref.lib.wref_split_z(depth, nb, first, count) == nb
+        table.append(np.concatenate([[depth, nb], first, count]).astype(np.int32))
+    out["split_table"] = np.concatenate(table)
+    save("formats", **out)
+
+
 if __name__ == "__main__":
+    if sys.argv[1:] == ["formats"]:
+        formats(O.Reference())
+        sys.exit(0)
     if os.environ.get("OMP_NUM_THREADS") != "1":
         print("run with OMP_NUM_THREADS=1", file=sys.stderr)
         sys.exit(2)

@@ -179,6 +179,64 @@ def test_flow_level_bitexact(setup, orc, tol, iters, nwarps):
         assert np.array_equal(host(a), b)
 
 
+def _smooth_random(rng, shape, passes=3):
+    a = rng.random(shape).astype(np.float32)
+    for _ in range(passes):
+        for ax in range(3):
+            a = (a + np.roll(a, 1, ax) + np.roll(a, -1, ax)) / np.float32(3)
+    return a.astype(np.float32)
+
+
+@pytest.mark.parametrize("form,zchunk", [(1, 0), (1, 5), (2, 0), (2, 3)])
+@pytest.mark.parametrize("dims", [(32, 32, 32), (37, 29, 23)])
+def test_flow_level_kernel_forms_bitexact(setup, orc, form, zchunk, dims):
+    """Fused and primal+dual forms, default and odd z-chunks, on a grid whose
+    sides are not multiples of the tile: every form matches the oracle bit for
+    bit through residual (50, 100) and Kty-store (49, 99) iterations."""
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    nx, ny, nz = dims
+    rng = np.random.default_rng(11)
+    I1 = _smooth_random(rng, (nz, ny, nx))
+    I2 = _smooth_random(rng, (nz, ny, nx))
+    V0 = (rng.normal(size=(3, nz, ny, nx)) * 0.7).astype(np.float32)
+    Y = [np.zeros((3, nz, ny, nx), np.float32) for _ in range(3)] + [np.zeros((nz, ny, nx), np.float32)]
+    aabb = np.array([0, nx, 0, ny, 0, nz], np.float32)
+    roi = [3, 4, 2, 5, 1, 3]
+    oV, oY = V0.copy(), [y.copy() for y in Y]
+    _, oits = orc.flow_level(list(dims), I1, I2, oV, *oY, 0.0, 0.05, 120, 2, aabb, roi, deterministic=1)
+    dV = dev(torch, V0)
+    dY = [dev(torch, y) for y in Y]
+    ctx.set_tuning("pd_form", form)
+    ctx.set_tuning("pd_zchunk", zchunk)
+    try:
+        its = ctx.flow_level(list(dims), dev(torch, I1), dev(torch, I2), dV, *dY, 0.0, 0.05, 120, 2, aabb, roi)
+        assert ctx.get_tuning(list(dims)) == (form, zchunk)
+    finally:
+        ctx.set_tuning("pd_form", 0)
+        ctx.set_tuning("pd_zchunk", 0)
+    assert list(its) == list(oits)
+    assert np.array_equal(host(dV), oV)
+    for a, b in zip(dY, oY):
+        assert np.array_equal(host(a), b)
+
+
+def test_flow_level_autotuned_plan(setup):
+    """The autotuner records a valid plan for a grid after its first level."""
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    dims = (40, 24, 20)
+    rng = np.random.default_rng(12)
+    I1 = _smooth_random(rng, dims[::-1])
+    I2 = _smooth_random(rng, dims[::-1])
+    V = torch.zeros((3,) + dims[::-1], device="cuda")
+    Y = [torch.zeros((3,) + dims[::-1], device="cuda") for _ in range(3)] + [torch.zeros(dims[::-1], device="cuda")]
+    aabb = np.array([0, dims[0], 0, dims[1], 0, dims[2]], np.float32)
+    ctx.flow_level(list(dims), dev(torch, I1), dev(torch, I2), V, *Y, 0.0, 0.05, 10, 1, aabb, [2] * 6)
+    form, zchunk = ctx.get_tuning(list(dims))
+    assert form in (1, 2) and 1 <= zchunk <= dims[2]
+
+
 def test_flow_multiscale_bitexact(setup, orc):
     s = setup
     torch, ctx = s["torch"], s["ctx"]

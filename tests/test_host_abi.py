@@ -12,11 +12,11 @@ import pytest
 import oracle as O
 import phantoms as P
 
-HDR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include", "wap", "wap.h")
+INC = os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include", "wap")
 
 
 def declared():
-    txt = open(HDR).read()
+    txt = "".join(open(os.path.join(INC, f)).read() for f in sorted(os.listdir(INC)) if f.endswith(".h"))
     return sorted(set(re.findall(r"WAP_API\s+[^;(]*?\b(wap_\w+)\s*\(", txt)))
 
 

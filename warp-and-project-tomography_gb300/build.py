@@ -40,7 +40,8 @@ def sources():
 
 def headers():
     hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".h")]
-    hs.append(os.path.join(REPO, "include", "wap", "wap.h"))
+    inc = os.path.join(REPO, "include", "wap")
+    hs += [os.path.join(inc, f) for f in os.listdir(inc) if f.endswith(".h")]
     return hs
 
 

@@ -111,7 +111,13 @@ struct wap_ctx {
 
   wap_stats stats{};
   int profiling = 0;
+  int pd_form = 0;    // 0: autotuned, 1: fused kernel, 2: primal + dual kernels
+  int pd_zchunk = 0;  // 0: autotuned / default
+  int rcp_ok = -1;    // __frcp_rn(x) == 1.0f/x over all floats (-1: not checked yet)
+  std::map<std::tuple<int, int, int>, std::pair<int, int>> pd_plans;  // grid -> (form, zchunk)
   std::map<uint32_t, int> fastdiv_ok;  // shrink divisor bits -> exhaustively verified
+  wap_observer_fn observer = nullptr;
+  void *observer_user = nullptr;
   std::vector<cudaEvent_t> pd_events;  // pairs, reused per 50-iteration chunk
   std::string err;
 };
@@ -166,6 +172,17 @@ void sart_order(int pstart, int pend, std::vector<int> &order) {
   order.resize(num);
   for (int i = 0; i < num; ++i) order[i] = (i % 2 == 0) ? pstart + i / 2 : pend - i / 2;
 }
+
+// Reports an intermediate state to the observer once the stream has
+// produced it.
+int notify(wap_ctx *ctx, int event, int a, int b, const float *d) {
+  if (!ctx->observer) return WAP_OK;
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->observer(ctx->observer_user, event, ctx->level, a, b, d);
+  return WAP_OK;
+}
+
+bool has_scan(const wap_ctx *ctx) { return ctx->nv > 0 && !ctx->h_geom.empty(); }
 
 int ensure_level_buffers(wap_ctx *ctx) {
   const size_t nv = ctx->nv, np = ctx->np, F = ctx->F;
@@ -422,6 +439,65 @@ FlowWork *flow_work(wap_ctx *ctx, const int dims[3]) {
   return p;
 }
 
+// The primal-dual iteration's kernel form and z-chunk for one grid: the
+// fused kernel or the primal + dual pair, each over a few z-chunks.  Both
+// forms compute identical bits, so the choice changes only speed.  Unless
+// forced (wap_set_tuning), the candidates are timed once per grid size with
+// CUDA events on the context's stream; a candidate launch only reads the
+// current iterate and writes the next-iterate buffers, which the real
+// iteration then overwrites, so tuning leaves the solver's state untouched.
+template <class Launch>
+int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zchunk) {
+  const int *n = D.n;
+  const auto key = std::make_tuple(n[0], n[1], n[2]);
+  // z-chunk defaults: about 4 waves of 2 fused blocks / 8 waves of 6 split
+  // blocks over the 152 SMs.
+  const int tiles_f = ((n[0] + 31) / 32) * ((n[1] + 6) / 7);
+  const int tiles_s = ((n[0] + 31) / 32) * ((n[1] + 7) / 8);
+  const int zf = std::max(2, std::min(64, n[2] * tiles_f / 1216));
+  const int zs = std::max(2, std::min(32, n[2] * tiles_s / 7296));
+  if (ctx->pd_form) {
+    form = ctx->pd_form;
+    zchunk = ctx->pd_zchunk ? ctx->pd_zchunk : (form == 1 ? zf : zs);
+    return WAP_OK;
+  }
+  auto it = ctx->pd_plans.find(key);
+  if (it != ctx->pd_plans.end()) {
+    form = it->second.first;
+    zchunk = it->second.second;
+    return WAP_OK;
+  }
+  std::vector<std::pair<int, int>> cand;
+  for (int z : {zf / 2, zf, zf * 2})
+    if (z >= 1 && z <= n[2]) cand.emplace_back(1, z);
+  for (int z : {zs / 2, zs, zs * 2, zs * 4})
+    if (z >= 1 && z <= n[2]) cand.emplace_back(2, z);
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  float best = 1e30f;
+  std::pair<int, int> pick = cand.front();
+  for (const auto &c : cand) {
+    KL(launch(c.first, c.second, 0, 0, 0));  // warm-up
+    CU(cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < 3; ++r) KL(launch(c.first, c.second, 0, 0, 0));
+    CU(cudaEventRecord(e1, ctx->stream));
+    CU(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    CU(cudaEventElapsedTime(&ms, e0, e1));
+    if (ms < best) {
+      best = ms;
+      pick = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->pd_plans[key] = pick;
+  form = pick.first;
+  zchunk = pick.second;
+  return WAP_OK;
+}
+
 // optical_flow::L1TVOpticalFlowNonlinear3D (optical_flow.h:88-995).
 // V (3 ch) is read and written whole; Y (10 ch: Y1,Y2,Y3,Y4) is read whole
 // and written on the ROI only, as the reference writes back.
@@ -445,9 +521,6 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   float *vcur = w->va.as<float>(), *vnext = w->vb.as<float>();
   float *y = w->y.as<float>();
   float *ycur = y, *ynext = w->y2.as<float>();
-  // z-chunk per block: at least ~4 waves of 2 resident blocks over 152 SMs.
-  const int tiles = ((dims[0] + 31) / 32) * ((dims[1] + 6) / 7);
-  const int zchunk = std::max(2, std::min(64, dims[2] * tiles / 1216));
   CU(cudaMemcpyAsync(vcur, V, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
   CU(cudaMemcpyAsync(vnext, V, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
   for (int q = 0; q < 3; ++q)
@@ -475,6 +548,26 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     fd = ctx->fastdiv_ok.emplace(den_bits, nbad == 0 ? 1 : 0).first;
   }
   const int fastdiv = fd->second;
+  if (ctx->rcp_ok < 0) {
+    DevMem bad;
+    CU(bad.ensure(sizeof(unsigned long long)));
+    KL(launch_pd_rcp_check(bad.as<unsigned long long>(), ctx->stream));
+    unsigned long long nbad = 1;
+    CU(cudaMemcpyAsync(&nbad, bad.p, sizeof(nbad), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    ctx->rcp_ok = nbad == 0 ? 1 : 0;
+  }
+  const int rcp = ctx->rcp_ok;
+  int form = 0, zchunk = 0;
+  auto pd_launch = [&](int f, int zc, int mode, int store, int res) -> cudaError_t {
+    if (f == 1)
+      return launch_pd_fused(D, zc, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
+                             w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, store, res, acc,
+                             ctx->stream);
+    return launch_pd_split(D, zc, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
+                           w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp, store, res, acc,
+                           ctx->stream);
+  };
   AdvectJob aj{vcur, I2, w->warp.as<float>(), -1.0f};
   for (int wi = 0; wi < nwarps; ++wi) {
     // advect I2 by the current flow, dt = -1 (optical_flow.h:418)
@@ -484,6 +577,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream));
     ctx->stats.advect_voxels += (double)nv;
     KL(launch_linearize(D, w->warp.as<float>(), I1, vcur, w->u.as<float>(), w->kx4prev.as<float>(), ctx->stream));
+    if (wi == 0 && max_iters >= 0) TRY(pd_plan(ctx, D, pd_launch, form, zchunk));
     int it = 0;
     float err = 1.0f;
     // Profile only the largest grid seen in this outer iteration.
@@ -511,8 +605,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
       if (res) CU(cudaMemsetAsync(acc, 0, sizeof(double) * 2, ctx->stream));
       if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending], ctx->stream));
       const int mode = (it == 1) ? (wi == 0 ? 1 : 2) : 0;
-      KL(launch_pd_fused(D, zchunk, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
-                         w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, store, res, acc, ctx->stream));
+      KL(pd_launch(form, zchunk, mode, store, res));
       if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending++ + 1], ctx->stream));
       std::swap(vcur, vnext);
       std::swap(ycur, ynext);
@@ -645,6 +738,70 @@ int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_
   return WAP_OK;
 }
 
+int wap_create_compute(wap_ctx **out, int device) {
+  if (!out) return WAP_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return WAP_ENODEV;
+  std::unique_ptr<wap_ctx> c(new wap_ctx);
+  wap_ctx *ctx = c.get();
+  ctx->device = device;
+  CU(cudaSetDevice(device));
+  CU(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  ctx->own_stream = true;
+  CU(ctx->maxbits.ensure(sizeof(unsigned)));
+  *out = c.release();
+  return WAP_OK;
+}
+
+int wap_alloc(wap_ctx *ctx, size_t bytes, void **d_out) {
+  CHECK(ctx && d_out, WAP_EINVAL, "null argument");
+  *d_out = nullptr;
+  CU(cudaSetDevice(ctx->device));
+  cudaError_t e = cudaMalloc(d_out, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    *d_out = nullptr;
+    return fail(ctx, WAP_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  }
+  return WAP_OK;
+}
+
+int wap_free(wap_ctx *ctx, void *d_ptr) {
+  CHECK(ctx, WAP_EINVAL, "null context");
+  if (d_ptr) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    CU(cudaFree(d_ptr));
+  }
+  return WAP_OK;
+}
+
+int wap_copy_to_device(wap_ctx *ctx, void *d_dst, const void *h_src, size_t bytes) {
+  CHECK(ctx && (bytes == 0 || (d_dst && h_src)), WAP_EINVAL, "null argument");
+  if (bytes) CU(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_copy_to_host(wap_ctx *ctx, void *h_dst, const void *d_src, size_t bytes) {
+  CHECK(ctx && (bytes == 0 || (h_dst && d_src)), WAP_EINVAL, "null argument");
+  if (bytes) CU(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+}
+
+int wap_fill_zero(wap_ctx *ctx, void *d_ptr, size_t bytes) {
+  CHECK(ctx && (bytes == 0 || d_ptr), WAP_EINVAL, "null argument");
+  if (bytes) CU(cudaMemsetAsync(d_ptr, 0, bytes, ctx->stream));
+  return WAP_OK;
+}
+
+int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user) {
+  CHECK(ctx, WAP_EINVAL, "null context");
+  ctx->observer = fn;
+  ctx->observer_user = user;
+  return WAP_OK;
+}
+
 void wap_destroy(wap_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
@@ -690,8 +847,33 @@ int wap_set_profiling(wap_ctx *ctx, int on) {
   return WAP_OK;
 }
 
+int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
+  CHECK(ctx && key, WAP_EINVAL, "null argument");
+  const std::string k = key;
+  if (k == "pd_form") {
+    CHECK(value >= 0 && value <= 2, WAP_EINVAL, "pd_form must be 0, 1 or 2");
+    ctx->pd_form = value;
+  } else if (k == "pd_zchunk") {
+    CHECK(value >= 0, WAP_EINVAL, "pd_zchunk must be >= 0");
+    ctx->pd_zchunk = value;
+  } else {
+    return fail(ctx, WAP_EINVAL, "unknown tuning key: " + k);
+  }
+  ctx->pd_plans.clear();
+  return WAP_OK;
+}
+
+int wap_get_tuning(wap_ctx *ctx, const int *dims, int *h_form, int *h_zchunk) {
+  CHECK(ctx && dims && h_form && h_zchunk, WAP_EINVAL, "null argument");
+  auto it = ctx->pd_plans.find(std::make_tuple(dims[0], dims[1], dims[2]));
+  *h_form = it == ctx->pd_plans.end() ? ctx->pd_form : it->second.first;
+  *h_zchunk = it == ctx->pd_plans.end() ? ctx->pd_zchunk : it->second.second;
+  return WAP_OK;
+}
+
 int wap_upload_projections(wap_ctx *ctx, const float *h_projs) {
   CHECK(ctx && h_projs, WAP_EINVAL, "null argument");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   const size_t n = ctx->np * ctx->scan.nproj;
   CU(ctx->projs_own.ensure(sizeof(float) * n));
   CU(cudaMemcpyAsync(ctx->projs_own.p, h_projs, sizeof(float) * n, cudaMemcpyHostToDevice, ctx->stream));
@@ -706,6 +888,7 @@ int wap_upload_projections(wap_ctx *ctx, const float *h_projs) {
 
 int wap_set_projections_device(wap_ctx *ctx, const float *d_projs) {
   CHECK(ctx && d_projs, WAP_EINVAL, "null argument");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   ctx->projs = d_projs;
   KL(launch_max_reduce(d_projs, ctx->np, ctx->maxbits.as<unsigned>(), ctx->stream));
   unsigned bits = 0;
@@ -750,6 +933,7 @@ int wap_level_frames(const wap_scan_desc *scan, int level, int *start, int *end,
 
 int wap_level_setup(wap_ctx *ctx, int level) {
   CHECK(ctx, WAP_EINVAL, "null context");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(level >= 0 && level <= 4, WAP_EINVAL, "level out of range");
   const int F = level_frames(ctx->scan.nframes_cli, ctx->scan.nproj, level, nullptr, nullptr, nullptr, nullptr, 0);
   ctx->st.assign(F, 0);
@@ -849,6 +1033,7 @@ int wap_forward_project(wap_ctx *ctx, int proj, const float *d_vol, float *d_img
 int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const float *const *h_d_vols,
                               float *const *h_d_imgs, float *const *h_d_lens, float *const *h_d_weights) {
   CHECK(ctx && h_proj && h_d_vols, WAP_EINVAL, "null argument");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(njobs >= 1 && njobs <= 65535, WAP_EINVAL, "job count out of range");
   std::vector<FpJob> jobs(njobs);
   for (int q = 0; q < njobs; ++q) {
@@ -872,6 +1057,7 @@ int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const 
 int wap_correction(wap_ctx *ctx, int n, const float *d_meas, const float *d_img, const float *d_len, float *d_dual,
                    float *d_corr) {
   CHECK(ctx && d_meas && d_img && d_len && d_corr, WAP_EINVAL, "null argument");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   KL(launch_correction(n, d_meas, d_img, d_len, d_dual, ctx->scan.alpha, d_corr, ctx->stream));
   return WAP_OK;
 }
@@ -879,6 +1065,7 @@ int wap_correction(wap_ctx *ctx, int n, const float *d_meas, const float *d_img,
 int wap_backproject_voxel(wap_ctx *ctx, int proj, const float *d_corr, const int *box, int mode, int exact,
                           float *d_vol) {
   CHECK(ctx && d_corr && box && d_vol, WAP_EINVAL, "null argument");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(proj >= 0 && proj < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
   CHECK(mode == 0 || mode == 1, WAP_EINVAL, "mode must be 0 or 1");
   for (int a = 0; a < 3; ++a)
@@ -900,6 +1087,7 @@ int wap_backproject_voxel(wap_ctx *ctx, int proj, const float *d_corr, const int
 
 int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_contrib, float *d_weight) {
   CHECK(ctx && d_corr && d_contrib && d_weight, WAP_EINVAL, "null argument");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(proj >= 0 && proj < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
   std::vector<SplatJob> jobs{SplatJob{d_corr, proj, d_contrib, d_weight}};
   TRY(upload(ctx, ctx->jobs_misc, jobs));
@@ -1020,6 +1208,7 @@ int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, in
     KL(launch_cp_primal(ca, ctx->ytp.as<float>(), ctx->ytv.as<float>(), ctx->vols.as<float>(), ctx->xprev.as<float>(),
                         ctx->stream));
     TRY(sart_frames(ctx, frames, sch->nb_sart, box, sch->bp_exact));
+    for (int f : frames) TRY(notify(ctx, WAP_EV_SART, f, icp, vol_ptr(ctx, f)));
     KL(launch_cp_overrelax(ca, ctx->vols.as<float>(), ctx->xprev.as<float>(), ctx->xbar.as<float>(), ctx->stream));
     ctx->stats.cp_frame_passes += ca.F;
   }
@@ -1027,10 +1216,12 @@ int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, in
   // (2) flow for each adjacent pair (WaP_Tomo.cpp:732-777)
   const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
   long long total = 0;
-  for (int f = f0; f < f1 && f + 1 < F; ++f)
+  for (int f = f0; f < f1 && f + 1 < F; ++f) {
     TRY(flow_multiscale(ctx, ctx->scan.vol, vol_ptr(ctx, f), vol_ptr(ctx, f + 1), flow_ptr(ctx, f), sch->flow_tol,
                         sch->flow_lambda, sch->flow_iters, sch->flow_warps, sch->flow_eta, sch->flow_sigma,
                         sch->flow_scales, cut6, flow_ptr(ctx, f), &total));
+    TRY(notify(ctx, WAP_EV_FLOW, f, 0, flow_ptr(ctx, f)));
+  }
   CU(cudaEventRecord(ev[2], ctx->stream));
   // (3) warp-and-project over each visited frame's window (WaP_Tomo.cpp:796-822)
   const int wend = std::min(f1, std::min(sch->wp_frames, F));
@@ -1047,6 +1238,7 @@ int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, in
         items.push_back(WapItem{f, ik, td});
       }
       TRY(wap_step(ctx, items, sch->bp_exact));
+      for (const WapItem &it : items) TRY(notify(ctx, WAP_EV_WARP, it.frame, it.proj, vol_ptr(ctx, it.frame)));
     }
   CU(cudaEventRecord(ev[3], ctx->stream));
   CU(cudaEventSynchronize(ev[3]));

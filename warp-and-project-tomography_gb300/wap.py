@@ -73,8 +73,20 @@ class Stats(ctypes.Structure):
     ]
 
 
+# wap_observer_fn: (user, event, level, a, b, d_data)
+OBSERVER = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                            ctypes.c_void_p)
+WAP_EV_SART, WAP_EV_FLOW, WAP_EV_WARP = 1, 2, 3
+
 # Every function declared in include/wap/wap.h, with its ctypes signature.
 SIGNATURES = {
+    "wap_create_compute": (_c_int, [ctypes.POINTER(_vp), _c_int]),
+    "wap_alloc": (_c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "wap_free": (_c_int, [_vp, _vp]),
+    "wap_copy_to_device": (_c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
+    "wap_copy_to_host": (_c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
+    "wap_fill_zero": (_c_int, [_vp, _vp, ctypes.c_size_t]),
+    "wap_set_observer": (_c_int, [_vp, OBSERVER, _vp]),
     "wap_create": (_c_int, [ctypes.POINTER(_vp), ctypes.POINTER(ScanDesc), _vp, _c_int]),
     "wap_destroy": (None, [_vp]),
     "wap_last_error": (ctypes.c_char_p, [_vp]),
@@ -82,6 +94,8 @@ SIGNATURES = {
     "wap_synchronize": (_c_int, [_vp]),
     "wap_get_stats": (_c_int, [_vp, ctypes.POINTER(Stats)]),
     "wap_set_profiling": (_c_int, [_vp, _c_int]),
+    "wap_set_tuning": (_c_int, [_vp, ctypes.c_char_p, _c_int]),
+    "wap_get_tuning": (_c_int, [_vp, _vp, _vp, _vp]),
     "wap_upload_projections": (_c_int, [_vp, _vp]),
     "wap_set_projections_device": (_c_int, [_vp, _vp]),
     "wap_gmax": (_c_float, [_vp]),
@@ -115,6 +129,13 @@ SIGNATURES = {
     "wap_projection_geometry": (_c_int, [ctypes.POINTER(ScanDesc), _c_double, _vp, _vp, _vp, _vp]),
     "wap_cg_screened_laplacian": (_c_int, [_vp, _vp, _c_float, _c_float, _vp, _vp, _c_float, _c_int, _c_float,
                                            _c_int, _vp]),
+    # include/wap/wap_io.h
+    "wap_analyze_info": (_c_int, [ctypes.c_char_p, _vp, _vp]),
+    "wap_analyze_load": (_c_int, [ctypes.c_char_p, _vp, ctypes.c_size_t]),
+    "wap_analyze_save": (_c_int, [ctypes.c_char_p, _vp, _vp, _vp]),
+    "wap_read_angles": (_c_int, [ctypes.c_char_p, _vp, _c_int, _vp]),
+    "wap_split_z": (_c_int, [_c_int, _c_int, _vp, _vp]),
+    "wap_lds_angles": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp]),
 }
 
 _lib = None
@@ -191,12 +212,36 @@ class Context:
     def __init__(self, scan, angles_deg, device=0):
         self.L = load()
         self.scan = scan
-        self.angles = np.ascontiguousarray(np.asarray(angles_deg, np.float64))
+        self._observer = None
         h = _vp()
-        r = self.L.wap_create(ctypes.byref(h), ctypes.byref(scan), self.angles.ctypes.data, device)
+        if scan is None:  # compute-only context (wap_create_compute)
+            self.angles = None
+            r = self.L.wap_create_compute(ctypes.byref(h), device)
+        else:
+            self.angles = np.ascontiguousarray(np.asarray(angles_deg, np.float64))
+            r = self.L.wap_create(ctypes.byref(h), ctypes.byref(scan), self.angles.ctypes.data, device)
         if r != WAP_OK:
             raise WapError("wap_create failed with status %d" % r)
         self.h = h
+
+    @classmethod
+    def compute(cls, device=0):
+        """A context without a scan, for the grid-argument calls."""
+        return cls(None, None, device)
+
+    def set_observer(self, fn):
+        """fn(event, level, a, b, d_data_ptr) or None."""
+        if fn is None:
+            self._observer = None
+            self.call("wap_set_observer", OBSERVER(), None)
+            return
+        self._observer = OBSERVER(lambda user, ev, lvl, a, b, d: fn(ev, lvl, a, b, d))
+        self.call("wap_set_observer", self._observer, None)
+
+    def copy_to_host(self, d_ptr, nfloats):
+        out = np.empty(nfloats, np.float32)
+        self.call("wap_copy_to_host", out.ctypes.data, d_ptr, out.nbytes)
+        return out
 
     def close(self):
         if getattr(self, "h", None):
@@ -267,6 +312,15 @@ class Context:
 
     def set_profiling(self, on):
         self.call("wap_set_profiling", 1 if on else 0)
+
+    def set_tuning(self, key, value):
+        self.call("wap_set_tuning", key.encode(), int(value))
+
+    def get_tuning(self, dims):
+        d = _ints(dims)
+        f, z = ctypes.c_int(0), ctypes.c_int(0)
+        self.call("wap_get_tuning", d.ctypes.data, ctypes.addressof(f), ctypes.addressof(z))
+        return f.value, z.value
 
     def set_stream(self, stream_ptr):
         self.call("wap_set_stream", stream_ptr)
@@ -362,3 +416,66 @@ def level_frames(scan, level):
     nf = L.wap_level_frames(ctypes.byref(scan), level, st.ctypes.data, en.ctypes.data, ft.ctypes.data,
                             ctypes.addressof(tu), 130)
     return nf, st[:nf].copy(), en[:nf].copy(), ft[:nf].copy(), tu.value
+
+
+# ---- host formats (include/wap/wap_io.h) -----------------------------------
+
+def _path(p):
+    return os.fsencode(p)
+
+
+def analyze_info(path):
+    """(W, H, D, C), Analyze datatype code."""
+    d = np.zeros(4, np.int32)
+    t = ctypes.c_int(0)
+    r = load().wap_analyze_info(_path(path), d.ctypes.data, ctypes.addressof(t))
+    if r != WAP_OK:
+        raise WapError("wap_analyze_info(%s) failed with status %d" % (path, r))
+    return tuple(int(v) for v in d), t.value
+
+
+def analyze_load(path):
+    """Float array of shape (C, D, H, W) (CImg order: x fastest)."""
+    (w, h, d, c), _ = analyze_info(path)
+    out = np.empty((c, d, h, w), np.float32)
+    r = load().wap_analyze_load(_path(path), out.ctypes.data, out.size)
+    if r != WAP_OK:
+        raise WapError("wap_analyze_load(%s) failed with status %d" % (path, r))
+    return out
+
+
+def analyze_save(path, arr, voxel_size=None):
+    """arr: (W,) .. (C, D, H, W) float array, CImg order."""
+    a = np.ascontiguousarray(arr, np.float32)
+    shp = list(a.shape[::-1]) + [1] * (4 - a.ndim)
+    dims = _ints(shp[:4])
+    vs = None if voxel_size is None else _floats(voxel_size)
+    r = load().wap_analyze_save(_path(path), a.ctypes.data, dims.ctypes.data, None if vs is None else vs.ctypes.data)
+    if r != WAP_OK:
+        raise WapError("wap_analyze_save(%s) failed with status %d" % (path, r))
+
+
+def read_angles(path, n):
+    out = np.zeros(n, np.float64)
+    got = ctypes.c_int(0)
+    r = load().wap_read_angles(_path(path), out.ctypes.data, n, ctypes.addressof(got))
+    if r != WAP_OK:
+        raise WapError("wap_read_angles(%s) failed with status %d" % (path, r))
+    return out, got.value
+
+
+def split_z(depth, nb):
+    first = np.zeros(nb, np.int32)
+    count = np.zeros(nb, np.int32)
+    r = load().wap_split_z(depth, nb, first.ctypes.data, count.ctypes.data)
+    if r != WAP_OK:
+        raise WapError("wap_split_z(%d, %d) failed with status %d" % (depth, nb, r))
+    return first, count
+
+
+def lds_angles(np_, ns=1, p=2, nz=50):
+    out = np.zeros(np_, np.float64)
+    r = load().wap_lds_angles(np_, ns, p, nz, out.ctypes.data)
+    if r != WAP_OK:
+        raise WapError("wap_lds_angles failed with status %d" % r)
+    return out
