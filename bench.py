@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--scales", type=int, default=4)
     ap.add_argument("--flow-iters", type=int, default=3000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-jobs", type=int, default=40,
+                    help="jobs of the served-form measurement added to the line (0: skip)")
+    ap.add_argument("--serve-rate", type=float, default=20.0)
+    ap.add_argument("--serve-workers", type=int, default=3)
     return ap.parse_args()
 
 
@@ -359,6 +363,15 @@ def run_gb300(args):
         sec, parts, sample = cpu_sample(args, counts, threads)
         result["cpu_baseline"] = {"value": 1.0 / sec, "unit": "outer-iter/s", "cores": threads, "kind": "port",
                                   "sample": sample, "component_seconds": parts}
+    if rank == 0 and world == 1 and args.serve_jobs > 0:
+        # Served form: p50/p95/p99 latency of a Poisson job stream through the
+        # request loop (see serving.py for the job mix).
+        import serving
+        del projs
+        ctx.close()
+        torch.cuda.empty_cache()
+        result["serving"] = serving.run(wap, torch, n_jobs=args.serve_jobs, rate=args.serve_rate,
+                                        workers=args.serve_workers)
     if rank == 0:
         print(json.dumps(result))
     if dist:

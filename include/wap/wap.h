@@ -236,6 +236,15 @@ WAP_API int wap_flow_multiscale(wap_ctx *ctx, const int *dims, const float *d_I1
                                 const float *d_V0, float tol, float lambda, int max_iters, int nwarps, float eta,
                                 float sigma, int scales, const int *cut6, float *d_Vout, long long *h_total_iters);
 
+/* The same with the dual fields' warm start (the reference's Y1..Y4
+ * arguments, resized to the coarsest level like V0; NULL for all four = zero,
+ * which is what PSART::Render passes). */
+WAP_API int wap_flow_multiscale_warm(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2,
+                                     const float *d_V0, const float *d_Y1, const float *d_Y2, const float *d_Y3,
+                                     const float *d_Y4, float tol, float lambda, int max_iters, int nwarps, float eta,
+                                     float sigma, int scales, const int *cut6, float *d_Vout,
+                                     long long *h_total_iters);
+
 /* ---- solver (context state) -------------------------------------------- */
 
 /* PSART::SART_Proximal_Operator (WaP_Tomo.cpp:1424-1678) on one frame of the
@@ -255,6 +264,15 @@ WAP_API int wap_outer_iteration(wap_ctx *ctx, const wap_schedule *sched, wap_sta
  * [0, F) is wap_outer_iteration; a single frame is one frame's share of the
  * iteration's work (the unit the throughput benchmark streams). */
 WAP_API int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sched, int f0, int f1, wap_stats *stats);
+
+/* The outer iteration as an ordered list of steps, for callers that
+ * interleave several reconstructions on one GPU: steps 0..n_cp-1 are the CP
+ * iterations over all frames (dual, primal, SART, over-relaxation), the next
+ * F-1 steps the flows of the pairs (f, f+1), the last the warp-and-project
+ * pass.  Running the steps 0..nsteps-1 in order is exactly
+ * wap_outer_iteration. */
+WAP_API int wap_outer_iteration_nsteps(const wap_ctx *ctx, const wap_schedule *sched);
+WAP_API int wap_outer_iteration_step(wap_ctx *ctx, const wap_schedule *sched, int step, wap_stats *stats);
 
 /* Per-projection matrices as the projector kernels use them (host only, no
  * GPU needed): the reference's PixelsToModel, ModelToVolume, model-view x

@@ -306,6 +306,34 @@ def test_outer_iteration_bitexact(setup, orc, wapmod):
         assert st.kernel_launches > 0
 
 
+def test_outer_iteration_steps_equal_the_whole(setup, wapmod):
+    """The step decomposition (CP iterations, flow pairs, WaP pass) run in
+    order gives the outer iteration's bits, with and without an observer."""
+    s = setup
+    ctx = s["ctx"]
+    sched = wapmod.reference_schedule(n_cp=2, nb_sart=2, wp_frames=2, flow_iters=40, flow_scales=2, flow_tol=0.0,
+                                      flow_warps=2)
+    F = ctx.level_setup(0)
+    ctx.outer_iteration(sched)
+    whole = [ctx.download_volume(f) for f in range(F)], [ctx.download_flow(f) for f in range(F)]
+    events = []
+    ctx.set_observer(lambda ev, lvl, a, b, d: events.append((ev, a, b)))
+    try:
+        F2 = ctx.level_setup(0)
+        n = ctx.outer_iteration_nsteps(sched)
+        assert F2 == F and n == 2 + (F - 1) + 1
+        for k in range(n):
+            ctx.outer_iteration_step(sched, k)
+    finally:
+        ctx.set_observer(None)
+    for f in range(F):
+        assert np.array_equal(ctx.download_volume(f), whole[0][f])
+        assert np.array_equal(ctx.download_flow(f), whole[1][f])
+    assert [e for e in events if e[0] == wapmod.WAP_EV_SART] == [(1, f, c) for c in (1, 2) for f in range(F)]
+    assert [e[1] for e in events if e[0] == wapmod.WAP_EV_FLOW] == list(range(F - 1))
+    assert len([e for e in events if e[0] == wapmod.WAP_EV_WARP]) > 0
+
+
 @pytest.mark.parametrize("mode", [0, 1])
 def test_cg_screened_laplacian(setup, orc, mode):
     s = setup

@@ -97,3 +97,22 @@ def test_reference_tree_live_pin(orc):
     oi, ol, ow = orc.forward(scan, ang[2], vol)
     ref.lib.wref_destroy()
     assert np.array_equal(ow, w) and np.array_equal(oi, i) and np.array_equal(ol, l)
+
+
+def test_job_footprint_grows_with_the_job(wapmod):
+    sched = wapmod.reference_schedule(n_cp=2, flow_scales=4)
+    small = wapmod.job_device_bytes(wapmod.make_scan((64,) * 3, (96, 96), 64, nframes_cli=8), sched)
+    big = wapmod.job_device_bytes(wapmod.make_scan((128,) * 3, (192, 192), 64, nframes_cli=8), sched)
+    more = wapmod.job_device_bytes(wapmod.make_scan((128,) * 3, (192, 192), 128, nframes_cli=16), sched)
+    assert 0 < small < big < more
+    # 256^3 x 192 projections, 48 frames: dominated by 13 floats per voxel per frame
+    full = wapmod.job_device_bytes(wapmod.make_scan((256,) * 3, (384, 384), 192, nframes_cli=48), sched)
+    assert 48 * 13 * 4 * 256 ** 3 < full < 1.3 * 48 * 13 * 4 * 256 ** 3
+
+
+def test_server_without_a_gpu_is_an_error(wapmod, torch_available=None):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(wapmod.WapError):
+        wapmod.Server(1 << 30, workers=1)

@@ -22,6 +22,8 @@ REPO = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "lib", "libwap_gb300.so")
+CLI_SRC = os.path.join(HERE, "cli", "wap_tomo.cpp")
+CLI = os.path.join(HERE, "lib", "wap_tomo")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
           "-I" + os.path.join(REPO, "include"), "-I" + CSRC]
@@ -77,7 +79,23 @@ def build(force=False, jobs=None, extra=()):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    build_cli(force)
     return LIB
+
+
+def build_cli(force=False):
+    """The headless command line (cli/wap_tomo.cpp) over the C++ facade,
+    linked against lib/libwap_gb300.so (found next to the binary)."""
+    deps = [CLI_SRC, LIB] + headers()
+    if not (force or _stale(CLI, deps)):
+        return CLI
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-I" + os.path.join(REPO, "include"), CLI_SRC, "-o", CLI,
+           "-L" + os.path.dirname(LIB), "-lwap_gb300", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("CLI build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    return CLI
 
 
 if __name__ == "__main__":

@@ -16,11 +16,13 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <tuple>
 #include <vector>
 
 #include "wap/wap.h"
+#include "wap/wap_serve.h"
 #include "wap_flow.h"
 #include "wap_geometry.h"
 #include "wap_internal.h"
@@ -58,6 +60,10 @@ struct DevMem {
 struct Status {
   int code;
 };
+
+// Exhaustive proofs of the fast division paths, per (device, key).
+std::mutex g_proof_mutex;
+std::map<std::pair<int, uint64_t>, int> g_proofs;
 
 // Flow-solver workspace for one grid size (reused across pairs and calls).
 struct FlowWork {
@@ -113,9 +119,7 @@ struct wap_ctx {
   int profiling = 0;
   int pd_form = 0;    // 0: autotuned, 1: fused kernel, 2: primal + dual kernels
   int pd_zchunk = 0;  // 0: autotuned / default
-  int rcp_ok = -1;    // __frcp_rn(x) == 1.0f/x over all floats (-1: not checked yet)
   std::map<std::tuple<int, int, int>, std::pair<int, int>> pd_plans;  // grid -> (form, zchunk)
-  std::map<uint32_t, int> fastdiv_ok;  // shrink divisor bits -> exhaustively verified
   wap_observer_fn observer = nullptr;
   void *observer_user = nullptr;
   std::vector<cudaEvent_t> pd_events;  // pairs, reused per 50-iteration chunk
@@ -537,32 +541,37 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   const float rinv = 1.0f / den;
   uint32_t den_bits;
   std::memcpy(&den_bits, &den, 4);
-  auto fd = ctx->fastdiv_ok.find(den_bits);
-  if (fd == ctx->fastdiv_ok.end()) {
+  // Proofs are per device and shared by every context in the process
+  // (key 0: the reciprocal; otherwise the divisor's bits).
+  auto proven = [&](uint64_t key, int &out) -> int {
+    {
+      std::lock_guard<std::mutex> lk(g_proof_mutex);
+      auto it = g_proofs.find(std::make_pair(ctx->device, key));
+      if (it != g_proofs.end()) {
+        out = it->second;
+        return WAP_OK;
+      }
+    }
     DevMem bad;
     CU(bad.ensure(sizeof(unsigned long long)));
-    KL(launch_pd_fastdiv_check(den, rinv, bad.as<unsigned long long>(), ctx->stream));
+    if (key == 0) KL(launch_pd_rcp_check(bad.as<unsigned long long>(), ctx->stream));
+    else KL(launch_pd_fastdiv_check(den, rinv, bad.as<unsigned long long>(), ctx->stream));
     unsigned long long nbad = 1;
     CU(cudaMemcpyAsync(&nbad, bad.p, sizeof(nbad), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
-    fd = ctx->fastdiv_ok.emplace(den_bits, nbad == 0 ? 1 : 0).first;
-  }
-  const int fastdiv = fd->second;
-  if (ctx->rcp_ok < 0) {
-    DevMem bad;
-    CU(bad.ensure(sizeof(unsigned long long)));
-    KL(launch_pd_rcp_check(bad.as<unsigned long long>(), ctx->stream));
-    unsigned long long nbad = 1;
-    CU(cudaMemcpyAsync(&nbad, bad.p, sizeof(nbad), cudaMemcpyDeviceToHost, ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
-    ctx->rcp_ok = nbad == 0 ? 1 : 0;
-  }
-  const int rcp = ctx->rcp_ok;
+    out = nbad == 0 ? 1 : 0;
+    std::lock_guard<std::mutex> lk(g_proof_mutex);
+    g_proofs[std::make_pair(ctx->device, key)] = out;
+    return WAP_OK;
+  };
+  int fastdiv = 0, rcp = 0;
+  TRY(proven(((uint64_t)1 << 32) | den_bits, fastdiv));
+  TRY(proven(0, rcp));
   int form = 0, zchunk = 0;
   auto pd_launch = [&](int f, int zc, int mode, int store, int res) -> cudaError_t {
     if (f == 1)
       return launch_pd_fused(D, zc, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
-                             w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, store, res, acc,
+                             w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp, store, res, acc,
                              ctx->stream);
     return launch_pd_split(D, zc, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
                            w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp, store, res, acc,
@@ -633,7 +642,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
 
 int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2, const float *V0, float tol,
                     float lambda, int max_iters, int nwarps, float eta, float sigma, int scales, const int cut6[6],
-                    float *Vout, long long *total) {
+                    float *Vout, long long *total, const float *const *Y0 = nullptr) {
   CHECK(scales >= 1 && scales <= 16, WAP_EINVAL, "scales out of range");
   const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
   // blurred inputs live in the two finest-level image buffers' sources
@@ -665,11 +674,24 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
   TRY(do_blur(ctx, dims, 1, sigma, I2, b2.as<float>()));
   for (int l = 0; l < scales; ++l) {
     PyramidLevel &P = *ctx->pyramid[l];
-    const size_t m = (size_t)P.d[0] * P.d[1] * P.d[2];
     TRY(do_resize(ctx, dims, 1, b1.as<float>(), P.d, P.i1.as<float>()));
     TRY(do_resize(ctx, dims, 1, b2.as<float>(), P.d, P.i2.as<float>()));
+  }
+  // Only the coarsest level starts from the arguments: every finer level's
+  // V and Y are replaced by the upsampled result of the level below
+  // (optical_flow.h:1101-1115) before they are used.
+  {
+    PyramidLevel &P = *ctx->pyramid[0];
+    const size_t m = (size_t)P.d[0] * P.d[1] * P.d[2];
     TRY(do_resize(ctx, dims, 3, V0, P.d, P.v.as<float>()));
-    CU(cudaMemsetAsync(P.y.p, 0, sizeof(float) * 10 * m, ctx->stream));
+    if (Y0) {
+      TRY(do_resize(ctx, dims, 3, Y0[0], P.d, P.y.as<float>()));
+      TRY(do_resize(ctx, dims, 3, Y0[1], P.d, P.y.as<float>() + 3 * m));
+      TRY(do_resize(ctx, dims, 3, Y0[2], P.d, P.y.as<float>() + 6 * m));
+      TRY(do_resize(ctx, dims, 1, Y0[3], P.d, P.y.as<float>() + 9 * m));
+    } else {
+      CU(cudaMemsetAsync(P.y.p, 0, sizeof(float) * 10 * m, ctx->stream));
+    }
   }
   const float aabb[6] = {0, (float)dims[0], 0, (float)dims[1], 0, (float)dims[2]};
   for (int l = 0; l < scales; ++l) {
@@ -691,6 +713,83 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
   return WAP_OK;
 }
 
+int check_schedule(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
+  CHECK(ctx && sch, WAP_EINVAL, "null argument");
+  CHECK(ctx->level >= 0, WAP_ESTATE, "no level set up");
+  CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
+  CHECK(0 <= f0 && f0 < f1 && f1 <= ctx->F, WAP_EINVAL, "frame range out of bounds");
+  CHECK(sch->cut >= 1 && 2 * sch->cut < ctx->scan.vol[0] && 2 * sch->cut < ctx->scan.vol[1] &&
+            2 * sch->cut < ctx->scan.vol[2],
+        WAP_EINVAL, "cut must leave a non-empty ROI and be at least 1");
+  CHECK(sch->n_cp >= 0 && sch->nb_sart >= 0 && sch->nb_projwarp >= 0 && sch->flow_iters >= 0 &&
+            sch->flow_warps >= 0 && sch->flow_scales >= 1,
+        WAP_EINVAL, "negative schedule count");
+  return WAP_OK;
+}
+
+// One CP iteration (number icp, 1-based) over frames [f0, f1): dual, primal,
+// SART proximal operator, over-relaxation (WaP_Tomo.cpp:563-690), each
+// batched over the frames.
+int cp_pass(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1, int icp) {
+  int box[6];
+  roi_box(ctx, sch->cut, box);
+  CpArgs ca;
+  for (int a = 0; a < 3; ++a) ca.n[a] = ctx->scan.vol[a];
+  std::memcpy(ca.box, box, sizeof(box));
+  ca.f0 = f0;
+  ca.F = f1 - f0;
+  ca.Ftot = ctx->F;
+  ca.sigma = (float)(.9 / (8.0f * 1.0f));
+  ca.tau = 1.0f;
+  ca.tv_w = (float)ctx->scan.tv_w;
+  ca.tp_w = (float)ctx->scan.tp_w;
+  ca.gmax = ctx->gmax;
+  std::vector<int> frames;
+  for (int f = f0; f < f1; ++f) frames.push_back(f);
+  KL(launch_cp_dual(ca, ctx->xbar.as<float>(), ctx->zero_vol.as<float>(), ctx->ytv.as<float>(),
+                    ctx->ytp.as<float>(), ctx->stream));
+  KL(launch_cp_primal(ca, ctx->ytp.as<float>(), ctx->ytv.as<float>(), ctx->vols.as<float>(), ctx->xprev.as<float>(),
+                      ctx->stream));
+  TRY(sart_frames(ctx, frames, sch->nb_sart, box, sch->bp_exact));
+  for (int f : frames) TRY(notify(ctx, WAP_EV_SART, f, icp, vol_ptr(ctx, f)));
+  KL(launch_cp_overrelax(ca, ctx->vols.as<float>(), ctx->xprev.as<float>(), ctx->xbar.as<float>(), ctx->stream));
+  ctx->stats.cp_frame_passes += ca.F;
+  return WAP_OK;
+}
+
+// The multiscale flow of the pair (f, f+1) (WaP_Tomo.cpp:732-777).
+int flow_pair(wap_ctx *ctx, const wap_schedule *sch, int f) {
+  const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
+  long long total = 0;
+  TRY(flow_multiscale(ctx, ctx->scan.vol, vol_ptr(ctx, f), vol_ptr(ctx, f + 1), flow_ptr(ctx, f), sch->flow_tol,
+                      sch->flow_lambda, sch->flow_iters, sch->flow_warps, sch->flow_eta, sch->flow_sigma,
+                      sch->flow_scales, cut6, flow_ptr(ctx, f), &total));
+  TRY(notify(ctx, WAP_EV_FLOW, f, 0, flow_ptr(ctx, f)));
+  return WAP_OK;
+}
+
+// Warp-and-project over the windows of the visited frames in [f0, f1)
+// (WaP_Tomo.cpp:796-822), batched over frames by window slot.
+int wap_pass(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
+  const int wend = std::min(f1, std::min(sch->wp_frames, ctx->F));
+  int maxnum = 0;
+  for (int f = f0; f < wend; ++f) maxnum = std::max(maxnum, ctx->en[f] - ctx->st[f] + 1);
+  for (int wp = 0; wp < sch->nb_projwarp; ++wp)
+    for (int s = 0; s < maxnum; ++s) {
+      std::vector<WapItem> items;
+      for (int f = f0; f < wend; ++f) {
+        const int ik = ctx->st[f] + s;
+        if (ik > ctx->en[f]) continue;
+        float td = (ik - ctx->ft[f]) / ctx->tunit;
+        td = mac_min(mac_max(-1.0f, td), 1.0f);
+        items.push_back(WapItem{f, ik, td});
+      }
+      TRY(wap_step(ctx, items, sch->bp_exact));
+      for (const WapItem &it : items) TRY(notify(ctx, WAP_EV_WARP, it.frame, it.proj, vol_ptr(ctx, it.frame)));
+    }
+  return WAP_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -702,8 +801,10 @@ int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_
   if (!out || !scan || !h_angles_deg) return WAP_EINVAL;
   *out = nullptr;
   for (int a = 0; a < 3; ++a)
-    if (scan->vol[a] < 3) return WAP_EINVAL;
-  if (scan->det[0] < 5 || scan->det[1] < 5 || scan->nproj < 1 || scan->nframes_cli < 1) return WAP_EINVAL;
+    if (scan->vol[a] < 3 || scan->vol[a] > 65535) return WAP_EINVAL;
+  if (scan->det[0] < 5 || scan->det[1] < 5 || scan->det[0] > 65535 || scan->det[1] > 65535 || scan->nproj < 1 ||
+      scan->nframes_cli < 1)
+    return WAP_EINVAL;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return WAP_ENODEV;
   std::unique_ptr<wap_ctx> c(new wap_ctx);
@@ -1146,6 +1247,21 @@ int wap_flow_multiscale(wap_ctx *ctx, const int *dims, const float *d_I1, const 
   return WAP_OK;
 }
 
+int wap_flow_multiscale_warm(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, const float *d_V0,
+                             const float *d_Y1, const float *d_Y2, const float *d_Y3, const float *d_Y4, float tol,
+                             float lambda, int max_iters, int nwarps, float eta, float sigma, int scales,
+                             const int *cut6, float *d_Vout, long long *h_total_iters) {
+  CHECK(ctx && dims && d_I1 && d_I2 && d_V0 && cut6 && d_Vout, WAP_EINVAL, "null argument");
+  CHECK((d_Y1 && d_Y2 && d_Y3 && d_Y4) || (!d_Y1 && !d_Y2 && !d_Y3 && !d_Y4), WAP_EINVAL,
+        "give all four dual fields or none");
+  long long tot = 0;
+  const float *Y0[4] = {d_Y1, d_Y2, d_Y3, d_Y4};
+  TRY(flow_multiscale(ctx, dims, d_I1, d_I2, d_V0, tol, lambda, max_iters, nwarps, eta, sigma, scales, cut6, d_Vout,
+                      &tot, d_Y1 ? Y0 : nullptr));
+  if (h_total_iters) *h_total_iters = tot;
+  return WAP_OK;
+}
+
 int wap_sart_prox(wap_ctx *ctx, int frame, int nb_sart, int cut, int exact) {
   CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
   CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
@@ -1170,76 +1286,19 @@ int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exa
 }
 
 int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1, wap_stats *stats) {
-  CHECK(ctx && sch, WAP_EINVAL, "null argument");
-  CHECK(ctx->level >= 0, WAP_ESTATE, "no level set up");
-  CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
-  CHECK(0 <= f0 && f0 < f1 && f1 <= ctx->F, WAP_EINVAL, "frame range out of bounds");
-  CHECK(sch->cut >= 1 && 2 * sch->cut < ctx->scan.vol[0] && 2 * sch->cut < ctx->scan.vol[1] &&
-            2 * sch->cut < ctx->scan.vol[2],
-        WAP_EINVAL, "cut must leave a non-empty ROI and be at least 1");
-  CHECK(sch->n_cp >= 0 && sch->nb_sart >= 0 && sch->nb_projwarp >= 0 && sch->flow_iters >= 0 &&
-            sch->flow_warps >= 0 && sch->flow_scales >= 1,
-        WAP_EINVAL, "negative schedule count");
+  TRY(check_schedule(ctx, sch, f0, f1));
   ctx->stats = wap_stats{};
-  ctx->stats.flow_pd_iterations = 0;
-  const int F = ctx->F;
-  int box[6];
-  roi_box(ctx, sch->cut, box);
   cudaEvent_t ev[4];
   for (auto &e : ev) CU(cudaEventCreate(&e));
   CU(cudaEventRecord(ev[0], ctx->stream));
   // (1) CP prior + SART proximal steps (WaP_Tomo.cpp:563-698)
-  CpArgs ca;
-  for (int a = 0; a < 3; ++a) ca.n[a] = ctx->scan.vol[a];
-  std::memcpy(ca.box, box, sizeof(box));
-  ca.f0 = f0;
-  ca.F = f1 - f0;
-  ca.Ftot = F;
-  ca.sigma = (float)(.9 / (8.0f * 1.0f));
-  ca.tau = 1.0f;
-  ca.tv_w = (float)ctx->scan.tv_w;
-  ca.tp_w = (float)ctx->scan.tp_w;
-  ca.gmax = ctx->gmax;
-  std::vector<int> frames;
-  for (int f = f0; f < f1; ++f) frames.push_back(f);
-  for (int icp = 1; icp <= sch->n_cp; ++icp) {
-    KL(launch_cp_dual(ca, ctx->xbar.as<float>(), ctx->zero_vol.as<float>(), ctx->ytv.as<float>(),
-                      ctx->ytp.as<float>(), ctx->stream));
-    KL(launch_cp_primal(ca, ctx->ytp.as<float>(), ctx->ytv.as<float>(), ctx->vols.as<float>(), ctx->xprev.as<float>(),
-                        ctx->stream));
-    TRY(sart_frames(ctx, frames, sch->nb_sart, box, sch->bp_exact));
-    for (int f : frames) TRY(notify(ctx, WAP_EV_SART, f, icp, vol_ptr(ctx, f)));
-    KL(launch_cp_overrelax(ca, ctx->vols.as<float>(), ctx->xprev.as<float>(), ctx->xbar.as<float>(), ctx->stream));
-    ctx->stats.cp_frame_passes += ca.F;
-  }
+  for (int icp = 1; icp <= sch->n_cp; ++icp) TRY(cp_pass(ctx, sch, f0, f1, icp));
   CU(cudaEventRecord(ev[1], ctx->stream));
   // (2) flow for each adjacent pair (WaP_Tomo.cpp:732-777)
-  const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
-  long long total = 0;
-  for (int f = f0; f < f1 && f + 1 < F; ++f) {
-    TRY(flow_multiscale(ctx, ctx->scan.vol, vol_ptr(ctx, f), vol_ptr(ctx, f + 1), flow_ptr(ctx, f), sch->flow_tol,
-                        sch->flow_lambda, sch->flow_iters, sch->flow_warps, sch->flow_eta, sch->flow_sigma,
-                        sch->flow_scales, cut6, flow_ptr(ctx, f), &total));
-    TRY(notify(ctx, WAP_EV_FLOW, f, 0, flow_ptr(ctx, f)));
-  }
+  for (int f = f0; f < f1 && f + 1 < ctx->F; ++f) TRY(flow_pair(ctx, sch, f));
   CU(cudaEventRecord(ev[2], ctx->stream));
   // (3) warp-and-project over each visited frame's window (WaP_Tomo.cpp:796-822)
-  const int wend = std::min(f1, std::min(sch->wp_frames, F));
-  int maxnum = 0;
-  for (int f = f0; f < wend; ++f) maxnum = std::max(maxnum, ctx->en[f] - ctx->st[f] + 1);
-  for (int wp = 0; wp < sch->nb_projwarp; ++wp)
-    for (int s = 0; s < maxnum; ++s) {
-      std::vector<WapItem> items;
-      for (int f = f0; f < wend; ++f) {
-        const int ik = ctx->st[f] + s;
-        if (ik > ctx->en[f]) continue;
-        float td = (ik - ctx->ft[f]) / ctx->tunit;
-        td = mac_min(mac_max(-1.0f, td), 1.0f);
-        items.push_back(WapItem{f, ik, td});
-      }
-      TRY(wap_step(ctx, items, sch->bp_exact));
-      for (const WapItem &it : items) TRY(notify(ctx, WAP_EV_WARP, it.frame, it.proj, vol_ptr(ctx, it.frame)));
-    }
+  TRY(wap_pass(ctx, sch, f0, f1));
   CU(cudaEventRecord(ev[3], ctx->stream));
   CU(cudaEventSynchronize(ev[3]));
   float ms[3];
@@ -1250,6 +1309,92 @@ int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, in
   ctx->stats.ms_wap = ms[2];
   if (stats) *stats = ctx->stats;
   return WAP_OK;
+}
+
+int wap_outer_iteration_nsteps(const wap_ctx *ctx, const wap_schedule *sch) {
+  if (!ctx || !sch || ctx->level < 0) return -1;
+  return sch->n_cp + std::max(ctx->F - 1, 0) + 1;
+}
+
+int wap_outer_iteration_step(wap_ctx *ctx, const wap_schedule *sch, int step, wap_stats *stats) {
+  TRY(check_schedule(ctx, sch, 0, ctx ? ctx->F : 0));
+  const int nflow = std::max(ctx->F - 1, 0);
+  CHECK(step >= 0 && step < sch->n_cp + nflow + 1, WAP_EINVAL, "step out of range");
+  ctx->stats = wap_stats{};
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  CU(cudaEventRecord(e0, ctx->stream));
+  int phase = 0;
+  if (step < sch->n_cp) {
+    TRY(cp_pass(ctx, sch, 0, ctx->F, step + 1));
+  } else if (step < sch->n_cp + nflow) {
+    phase = 1;
+    TRY(flow_pair(ctx, sch, step - sch->n_cp));
+  } else {
+    phase = 2;
+    TRY(wap_pass(ctx, sch, 0, ctx->F));
+  }
+  CU(cudaEventRecord(e1, ctx->stream));
+  CU(cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  CU(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  (phase == 0 ? ctx->stats.ms_cp : phase == 1 ? ctx->stats.ms_flow : ctx->stats.ms_wap) = ms;
+  if (stats) *stats = ctx->stats;
+  return WAP_OK;
+}
+
+size_t wap_ctx_device_bytes(const wap_ctx *ctx) {
+  if (!ctx) return 0;
+  size_t b = 0;
+  for (const DevMem *m : {&ctx->geom, &ctx->projs_own, &ctx->vols, &ctx->flows, &ctx->ytv, &ctx->ytp, &ctx->xbar,
+                          &ctx->xprev, &ctx->zero_vol, &ctx->dual, &ctx->corr, &ctx->warped, &ctx->delta, &ctx->back,
+                          &ctx->jobs_fp, &ctx->jobs_bp, &ctx->jobs_adv, &ctx->jobs_acc, &ctx->jobs_misc, &ctx->world,
+                          &ctx->maxbits, &ctx->blur_a, &ctx->blur_b, &ctx->rs_a, &ctx->rs_b, &ctx->cg_buf})
+    b += m->bytes;
+  for (const auto &kv : ctx->flow_work) {
+    const FlowWork &w = *kv.second;
+    for (const DevMem *m : {&w.va, &w.vb, &w.y, &w.y2, &w.u, &w.kty, &w.kx4prev, &w.warp, &w.acc, &w.err, &w.world})
+      b += m->bytes;
+  }
+  for (const auto &p : ctx->pyramid)
+    if (p)
+      for (const DevMem *m : {&p->i1, &p->i2, &p->v, &p->y}) b += m->bytes;
+  for (const auto &kv : ctx->resize_tables)
+    for (int q = 0; q < 5; ++q) b += kv.second[q].bytes;
+  return b;
+}
+
+size_t wap_job_device_bytes(const wap_scan_desc *scan, const wap_schedule *sch) {
+  if (!scan || !sch) return 0;
+  const size_t nv = (size_t)scan->vol[0] * scan->vol[1] * scan->vol[2];
+  const size_t np = (size_t)scan->det[0] * scan->det[1];
+  const int F = level_frames(scan->nframes_cli, scan->nproj, 0, nullptr, nullptr, nullptr, nullptr, 0);
+  if (F <= 0) return 0;
+  std::vector<int> st(F), en(F);
+  std::vector<float> ft(F);
+  float tu = 0.0f;
+  level_frames(scan->nframes_cli, scan->nproj, 0, st.data(), en.data(), ft.data(), &tu, F);
+  size_t maxwin = 0;
+  for (int f = 0; f < F; ++f) maxwin = std::max(maxwin, (size_t)(en[f] - st[f] + 1));
+  size_t floats = 3 * nv                        // zero flow
+                  + np * scan->nproj            // projection stack
+                  + (size_t)F * 13 * nv         // volumes, flows, CP state, WaP scratch
+                  + (size_t)F * np * (1 + maxwin);  // corrections and dual rows
+  // flow: per pyramid level 35 floats/voxel of solver state + 15 of pyramid
+  // buffers; resize scratch (10 channels, twice) and blur scratch at full size
+  float t_eta = 1.0f;
+  for (int l = 0; l < std::max(sch->flow_scales, 1); ++l) {
+    size_t m = 1;
+    for (int a = 0; a < 3; ++a) m *= (size_t)std::max(1, (int)(scan->vol[a] * t_eta));
+    floats += 50 * m;
+    t_eta *= sch->flow_eta;
+  }
+  floats += 24 * nv;
+  const size_t tables = (size_t)scan->nproj * sizeof(ProjGeom) + (size_t)4 * 1024 * 1024;  // geometry, job tables
+  return floats * sizeof(float) + tables;
 }
 
 int wap_outer_iteration(wap_ctx *ctx, const wap_schedule *sch, wap_stats *stats) {

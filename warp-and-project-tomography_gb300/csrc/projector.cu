@@ -254,11 +254,31 @@ __device__ __forceinline__ float cubic_fast(float p0, float p1, float p2, float 
   return __fmaf_rn(0.5f * x, outer, p1);
 }
 
+// Index <-> float conversions without the conversion instructions (on this
+// part they issue to a low-rate pipe): exact for 0 <= i < 2^23, and for
+// 0 <= v < 2^22 respectively, which the callers guarantee.
+__device__ __forceinline__ float small_i2f(int i) { return __int_as_float(0x4B000000 | i) - 8388608.0f; }
+// floor(v) as float, for 0 <= v < 2^22: v + 2^23 rounds to the nearest
+// integer exactly, and one correction step gives the floor.
+__device__ __forceinline__ float small_floor(float v) {
+  const float r = (v + 8388608.0f) - 8388608.0f;
+  return r > v ? r - 1.0f : r;
+}
+__device__ __forceinline__ int small_f2i(float fl) { return __float_as_int(fl + 8388608.0f) - 0x4B000000; }
+
+// The host passes the scalars in both precisions (halfWf/halfHf/dsf/alphaf
+// are the float roundings); float_ok says halfW, halfH and ds are exact
+// floats, so that a single double operation rounded to float equals the
+// float operation.  The pixel test px < 2 || px >= W-2 on px = (int)_px is
+// the same as !(2 <= _px < W-2) for every float _px (NaN included), and for
+// _px inside that range (int)_px = floor(_px).
 template <bool kExact, int kMode>
 __global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restrict__ geom,
                                                        const BpJob *__restrict__ jobs, int zblocks, int nx, int ny,
                                                        int W, int H, double halfW, double halfH, float sdd,
-                                                       double ds, int float_ok, double alpha, float gmax) {
+                                                       double ds, int float_ok, double alpha, float gmax,
+                                                       float halfWf, float halfHf, float dsf, float alphaf,
+                                                       float wlim, float hlim) {
   const int jb = blockIdx.z / zblocks;
   const BpJob job = jobs[jb];
   const int x = job.box[0] + blockIdx.x * blockDim.x + threadIdx.x;
@@ -267,26 +287,25 @@ __global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restric
   if (x >= job.box[1] || y >= job.box[3] || z >= job.box[5]) return;
   const ProjGeom &g = geom[job.proj];
   float det[4];
-  mat4_vec(g.mvv2m, (float)x, (float)y, (float)z, 1.0f, det);
+  mat4_vec(g.mvv2m, small_i2f(x), small_i2f(y), small_i2f(z), 1.0f, det);
   const float qx = (det[0] / det[2]) * sdd;
   const float qy = (det[1] / det[2]) * sdd;
   float _px, _py;
   if (float_ok) {
-    // halfW, halfH and ds are exact floats here, and a single double
-    // operation rounded to float equals the float operation.
-    _px = (float)halfW - qx;
-    _py = (float)halfH - qy;
-    _px = _px / (float)ds;
-    _py = _py / (float)ds;
+    _px = halfWf - qx;
+    _py = halfHf - qy;
+    _px = _px / dsf;
+    _py = _py / dsf;
   } else {
     _px = (float)(halfW - (double)qx);
     _py = (float)(halfH - (double)qy);
     _px = (float)((double)_px / ds);
     _py = (float)((double)_py / ds);
   }
-  const int px = (int)_px, py = (int)_py;
-  const float dx = _px - (float)px, dy = _py - (float)py;
-  if (px < 2 || px >= W - 2 || py < 2 || py >= H - 2) return;
+  if (!(_px >= 2.0f && _px < wlim && _py >= 2.0f && _py < hlim)) return;
+  const float fx = small_floor(_px), fy = small_floor(_py);
+  const int px = small_f2i(fx), py = small_f2i(fy);
+  const float dx = _px - fx, dy = _py - fy;
   const float *__restrict__ pC = job.corr + py * W + px;
   float arr[4];
 #pragma unroll
@@ -299,7 +318,7 @@ __global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restric
                           : cubic_fast(arr[0], arr[1], arr[2], arr[3], dx);
   float *v = job.vol + (x + nx * (y + ny * z));
   if (kMode == 0) {
-    float nv = kExact ? (float)((double)*v + alpha * (double)gv) : __fmaf_rn((float)alpha, gv, *v);
+    float nv = kExact ? (float)((double)*v + alpha * (double)gv) : __fmaf_rn(alphaf, gv, *v);
     nv = mac_max(mac_min(gmax, nv), 0.0f);
     *v = nv;
   } else {
@@ -340,9 +359,12 @@ cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njo
   const int zblocks = (maxbox[2] + 1) / 2;
   const dim3 grid((maxbox[0] + 31) / 32, (maxbox[1] + 3) / 4, zblocks * njobs);
   const int float_ok = ((double)(float)halfW == halfW && (double)(float)halfH == halfH && (double)(float)ds == ds);
+  if (W >= (1 << 22) || H >= (1 << 22)) return cudaErrorInvalidValue;
+  const float wlim = (float)(W - 2), hlim = (float)(H - 2);
 #define WAP_BP(E, M)                                                                                             \
   bp_voxel_kernel<E, M><<<grid, block, 0, st>>>(d_geom, d_jobs, zblocks, dims[0], dims[1], W, H, halfW, halfH, sdd, \
-                                                ds, float_ok, alpha, gmax)
+                                                ds, float_ok, alpha, gmax, (float)halfW, (float)halfH, (float)ds,  \
+                                                (float)alpha, wlim, hlim)
   if (exact) {
     if (mode == 0) WAP_BP(true, 0);
     else WAP_BP(true, 1);

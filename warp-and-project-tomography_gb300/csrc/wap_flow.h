@@ -37,10 +37,10 @@ cudaError_t launch_linearize(const FlowDims &D, const float *warp, const float *
                              float *kx4prev, cudaStream_t st);
 cudaError_t launch_pd_fused(const FlowDims &D, int zchunk, const float *yin, float *yout, const float *u,
                             const float *vin, float *vout, float *kty, const float *kx4prev, int kxold_mode,
-                            float lambda, float sigma1, float rinv, int fastdiv, int store_kty, int residual,
+                            float lambda, float sigma1, float rinv, int fastdiv, int rcp, int store_kty, int residual,
                             double *acc, cudaStream_t st);
 // The same iteration as two kernels (primal, then dual); identical results.
-// rcp = 1 computes 1/x with the correctly rounded reciprocal.
+// rcp = 1 computes 1/x with the verified fast reciprocal.
 cudaError_t launch_pd_split(const FlowDims &D, int zchunk, const float *yin, float *yout, const float *u,
                             const float *vin, float *vout, float *kty, const float *kx4prev, int kxold_mode,
                             float lambda, float sigma1, float rinv, int fastdiv, int rcp, int store_kty,
@@ -48,7 +48,7 @@ cudaError_t launch_pd_split(const FlowDims &D, int zchunk, const float *yin, flo
 // Counts the float inputs for which the FMA-corrected division by den differs
 // from IEEE division (0 proves the fast path exact for this den).
 cudaError_t launch_pd_fastdiv_check(float den, float rinv, unsigned long long *d_bad, cudaStream_t st);
-// Counts the float inputs for which __frcp_rn(x) differs from 1.0f / x.
+// Counts the float inputs for which the fast reciprocal differs from 1.0f / x.
 cudaError_t launch_pd_rcp_check(unsigned long long *d_bad, cudaStream_t st);
 cudaError_t launch_residual_finish(const double *acc, int nPx, float *err, cudaStream_t st);
 cudaError_t launch_roi_copy(const FlowDims &D, int nch, const float *src, float *dst, cudaStream_t st);

@@ -1,0 +1,109 @@
+"""Served form: a seeded Poisson stream of reconstruction jobs of uneven sizes
+through the request loop (wap.Server, include/wap/wap_serve.h).
+
+Job mix (the served workload): volume sides drawn from {64, 96, 128, 192,
+256} with weights 0.3/0.25/0.2/0.15/0.1, projection counts from {64, 128,
+192}, detector side 1.5x the volume side, ellipsoid phantoms generated on the
+device, arrivals at a mean rate per second (seed 3).  Each job is one outer
+iteration of the reconstruction at time level 0 with frames = projections /
+8, 2 CP iterations x 2 SART sweeps, a 2-level flow of 20 primal-dual
+iterations and 1 warp per level, and the FP32 backprojection.  All inputs are
+generated before the arrival clock starts; latency is submit -> results on the
+host, on the server's clock.
+"""
+import time
+
+import numpy as np
+
+SIZES = (64, 96, 128, 192, 256)
+WEIGHTS = (0.3, 0.25, 0.2, 0.15, 0.1)
+NPROJS = (64, 128, 192)
+
+
+def job_stream(n_jobs, rate, seed=3, max_side=256):
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=n_jobs)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    sides = rng.choice(SIZES, size=n_jobs, p=WEIGHTS)
+    sides = np.minimum(sides, max_side)
+    nprojs = rng.choice(NPROJS, size=n_jobs)
+    return [dict(t=float(t), n=int(n), nproj=int(p), seed=1000 + i)
+            for i, (t, n, p) in enumerate(zip(arrivals, sides, nprojs))]
+
+
+def served_schedule(wap, frames):
+    s = wap.reference_schedule(n_cp=2, nb_sart=2, wp_frames=frames, flow_iters=20, flow_scales=2, flow_tol=0.0,
+                               flow_warps=1, bp_exact=0)
+    return s
+
+
+def _phantom(torch, n, seed, count=12):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    ax = torch.arange(n, device="cuda", dtype=torch.float32)
+    z, y, x = torch.meshgrid(ax, ax, ax, indexing="ij")
+    vol = torch.zeros((n, n, n), device="cuda")
+    for _ in range(count):
+        c = (0.15 + 0.7 * torch.rand(3, device="cuda", generator=g)) * n
+        r = (3.0 + 13.0 * torch.rand(3, device="cuda", generator=g)) * (n / 64.0)
+        d = ((x - c[0]) / r[0]) ** 2 + ((y - c[1]) / r[1]) ** 2 + ((z - c[2]) / r[2]) ** 2
+        vol += (d <= 1.0).float() * (0.1 + 0.9 * torch.rand(1, device="cuda", generator=g))
+    return vol
+
+
+def make_job(wap, torch, spec):
+    """Scan, schedule, angles and host projections of one job."""
+    n, nproj = spec["n"], spec["nproj"]
+    det = int(round(1.5 * n))
+    frames = max(1, nproj // 8)
+    scan = wap.make_scan((n, n, n), (det, det), nproj, nframes_cli=frames)
+    ang = (np.arange(nproj, dtype=np.float64) * 360.0 * 0.6180339887) % 360.0
+    vol = _phantom(torch, n, spec["seed"])
+    torch.cuda.synchronize()  # the context's stream does not wait on torch's
+    ctx = wap.Context(scan, ang)
+    try:
+        projs = torch.empty((nproj, det, det), device="cuda")
+        for k in range(nproj):
+            ctx.forward(k, vol, projs[k])
+        ctx.synchronize()
+        host = projs.cpu().numpy()
+    finally:
+        ctx.close()
+    return dict(scan=scan, sched=served_schedule(wap, frames), angles=ang, projs=host, n=n)
+
+
+def run(wap, torch, n_jobs=40, rate=20.0, budget_gb=150.0, workers=3, seed=3, max_side=256):
+    specs = job_stream(n_jobs, rate, seed, max_side)
+    jobs = [make_job(wap, torch, s) for s in specs]
+    torch.cuda.synchronize()
+    budget = int(budget_gb * (1 << 30))
+    srv = wap.Server(budget, workers=workers)
+    try:
+        start = time.perf_counter()
+        ids = []
+        for s, j in zip(specs, jobs):
+            delay = s["t"] - (time.perf_counter() - start)
+            if delay > 0:
+                time.sleep(delay)
+            ids.append(srv.submit(j["scan"], j["sched"], j["angles"], j["projs"], outer_iterations=1))
+        for jid in ids:
+            if srv.wait(jid, 3600.0) != wap.WAP_OK:
+                raise wap.WapError("served job %d failed" % jid)
+        infos = [srv.info(jid) for jid in ids]
+        _, peak = srv.memory()
+        for jid in ids:
+            srv.release(jid)
+    finally:
+        srv.close()
+    lat = np.array([i.t_done - i.t_submit for i in infos])
+    wait = np.array([i.t_admit - i.t_submit for i in infos])
+    span = max(i.t_done for i in infos) - min(i.t_submit for i in infos)
+    return {
+        "jobs": n_jobs, "arrival_rate_per_s": rate, "workers": workers, "budget_gb": budget_gb,
+        "throughput_jobs_per_s": n_jobs / span,
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p95": float(np.percentile(lat, 95)),
+                      "p99": float(np.percentile(lat, 99)), "mean": float(lat.mean())},
+        "admission_wait_s_mean": float(wait.mean()),
+        "peak_reserved_gb": peak / float(1 << 30),
+        "sides": {str(k): int(sum(1 for s in specs if s["n"] == k)) for k in SIZES},
+        "job": "1 outer iteration, frames = projections/8, 2 CP x 2 SART, 2-level flow x 20 PD its, FP32 BP",
+    }

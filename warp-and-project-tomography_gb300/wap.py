@@ -73,6 +73,18 @@ class Stats(ctypes.Structure):
     ]
 
 
+class JobDesc(ctypes.Structure):
+    _fields_ = [("scan", ScanDesc), ("sched", Schedule), ("outer_iterations", _c_int),
+                ("h_angles", _vp), ("h_projs", _vp)]
+
+
+class JobInfo(ctypes.Structure):
+    _fields_ = [("state", _c_int), ("status", _c_int), ("t_submit", _c_double), ("t_admit", _c_double),
+                ("t_done", _c_double), ("steps", ctypes.c_longlong), ("device_bytes", ctypes.c_size_t)]
+
+
+WAP_JOB_QUEUED, WAP_JOB_RUNNING, WAP_JOB_DONE, WAP_JOB_FAILED = range(4)
+
 # wap_observer_fn: (user, event, level, a, b, d_data)
 OBSERVER = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                             ctypes.c_void_p)
@@ -122,13 +134,29 @@ SIGNATURES = {
                                 _vp, _vp, _vp]),
     "wap_flow_multiscale": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_float, _c_float, _c_int, _c_int, _c_float,
                                      _c_float, _c_int, _vp, _vp, _vp]),
+    "wap_flow_multiscale_warm": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_float, _c_float, _c_int,
+                                          _c_int, _c_float, _c_float, _c_int, _vp, _vp, _vp]),
     "wap_sart_prox": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int]),
     "wap_warp_and_project": (_c_int, [_vp, _c_int, _c_int, _c_float, _c_int]),
     "wap_outer_iteration": (_c_int, [_vp, ctypes.POINTER(Schedule), ctypes.POINTER(Stats)]),
     "wap_outer_iteration_frames": (_c_int, [_vp, ctypes.POINTER(Schedule), _c_int, _c_int, ctypes.POINTER(Stats)]),
+    "wap_outer_iteration_nsteps": (_c_int, [_vp, ctypes.POINTER(Schedule)]),
+    "wap_outer_iteration_step": (_c_int, [_vp, ctypes.POINTER(Schedule), _c_int, ctypes.POINTER(Stats)]),
     "wap_projection_geometry": (_c_int, [ctypes.POINTER(ScanDesc), _c_double, _vp, _vp, _vp, _vp]),
     "wap_cg_screened_laplacian": (_c_int, [_vp, _vp, _c_float, _c_float, _vp, _vp, _c_float, _c_int, _c_float,
                                            _c_int, _vp]),
+    # include/wap/wap_serve.h
+    "wap_job_device_bytes": (ctypes.c_size_t, [ctypes.POINTER(ScanDesc), ctypes.POINTER(Schedule)]),
+    "wap_ctx_device_bytes": (ctypes.c_size_t, [_vp]),
+    "wap_server_create": (_c_int, [ctypes.POINTER(_vp), _c_int, ctypes.c_size_t, _c_int]),
+    "wap_server_destroy": (None, [_vp]),
+    "wap_server_submit": (_c_int, [_vp, ctypes.POINTER(JobDesc), ctypes.POINTER(ctypes.c_longlong)]),
+    "wap_server_info": (_c_int, [_vp, ctypes.c_longlong, ctypes.POINTER(JobInfo)]),
+    "wap_server_wait": (_c_int, [_vp, ctypes.c_longlong, _c_double]),
+    "wap_server_result": (_c_int, [_vp, ctypes.c_longlong, _c_int, _vp]),
+    "wap_server_release": (_c_int, [_vp, ctypes.c_longlong]),
+    "wap_server_now": (_c_double, [_vp]),
+    "wap_server_memory": (_c_int, [_vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     # include/wap/wap_io.h
     "wap_analyze_info": (_c_int, [ctypes.c_char_p, _vp, _vp]),
     "wap_analyze_load": (_c_int, [ctypes.c_char_p, _vp, ctypes.c_size_t]),
@@ -389,6 +417,14 @@ class Context:
         self.call("wap_outer_iteration_frames", ctypes.byref(sched), f0, f1, ctypes.byref(st))
         return st
 
+    def outer_iteration_nsteps(self, sched):
+        return self.L.wap_outer_iteration_nsteps(self.h, ctypes.byref(sched))
+
+    def outer_iteration_step(self, sched, step):
+        st = Stats()
+        self.call("wap_outer_iteration_step", ctypes.byref(sched), int(step), ctypes.byref(st))
+        return st
+
     def cg_screened_laplacian(self, dims, a, b, d_rhs, d_x, rel_tol=1e-6, max_iters=500, abs_tol=1e-9, mode=0):
         d = _ints(dims)
         it = _c_int(0)
@@ -479,3 +515,71 @@ def lds_angles(np_, ns=1, p=2, nz=50):
     if r != WAP_OK:
         raise WapError("wap_lds_angles failed with status %d" % r)
     return out
+
+
+# ---- request loop (include/wap/wap_serve.h) ----------------------------------
+
+def job_device_bytes(scan, sched):
+    return int(load().wap_job_device_bytes(ctypes.byref(scan), ctypes.byref(sched)))
+
+
+class Server:
+    """Many reconstructions on one GPU, admitted by device footprint."""
+
+    def __init__(self, budget_bytes, workers=2, device=0):
+        self.L = load()
+        h = _vp()
+        r = self.L.wap_server_create(ctypes.byref(h), device, int(budget_bytes), int(workers))
+        if r != WAP_OK:
+            raise WapError("wap_server_create failed with status %d" % r)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wap_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, scan, sched, angles, projs, outer_iterations=1):
+        a = np.ascontiguousarray(angles, np.float64)
+        p = np.ascontiguousarray(projs, np.float32)
+        d = JobDesc(scan=scan, sched=sched, outer_iterations=int(outer_iterations), h_angles=a.ctypes.data,
+                    h_projs=p.ctypes.data)
+        jid = ctypes.c_longlong(0)
+        r = self.L.wap_server_submit(self.h, ctypes.byref(d), ctypes.byref(jid))
+        if r != WAP_OK:
+            raise WapError("wap_server_submit failed with status %d" % r)
+        return jid.value
+
+    def info(self, jid):
+        i = JobInfo()
+        r = self.L.wap_server_info(self.h, jid, ctypes.byref(i))
+        if r != WAP_OK:
+            raise WapError("wap_server_info failed with status %d" % r)
+        return i
+
+    def wait(self, jid, timeout=600.0):
+        return self.L.wap_server_wait(self.h, jid, float(timeout))
+
+    def result(self, jid, frame, vol_shape):
+        out = np.empty(vol_shape, np.float32)
+        r = self.L.wap_server_result(self.h, jid, frame, out.ctypes.data)
+        if r != WAP_OK:
+            raise WapError("wap_server_result failed with status %d" % r)
+        return out
+
+    def release(self, jid):
+        return self.L.wap_server_release(self.h, jid)
+
+    def now(self):
+        return self.L.wap_server_now(self.h)
+
+    def memory(self):
+        a, b = ctypes.c_size_t(0), ctypes.c_size_t(0)
+        self.L.wap_server_memory(self.h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
