@@ -68,8 +68,11 @@ std::map<std::pair<int, uint64_t>, int> g_proofs;
 // Flow-solver workspace for one grid size (reused across pairs and calls).
 struct FlowWork {
   int n[3] = {0, 0, 0};
-  DevMem va, vb, y, y2, u, kty, kx4prev, warp, acc, err, world;
+  DevMem va, vb, y, y2, u, kty, kx4prev, warp, acc, err, world, tma_err;
   float aabb_key[6] = {0, 0, 0, 0, 0, 0};
+  // Tensor maps of the TMA-fed form: y over (y, y2), v over (va, vb), u.
+  int tma_state = 0;  // 0: not made, 1: made, -1: unavailable for this grid
+  PdTmaMap ymap[2], vmap[2], umap;
 };
 
 // Multiscale pyramid buffers for one finest size.
@@ -451,7 +454,7 @@ FlowWork *flow_work(wap_ctx *ctx, const int dims[3]) {
 // current iterate and writes the next-iterate buffers, which the real
 // iteration then overwrites, so tuning leaves the solver's state untouched.
 template <class Launch>
-int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zchunk) {
+int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zchunk, bool tma) {
   const int *n = D.n;
   const auto key = std::make_tuple(n[0], n[1], n[2]);
   // z-chunk defaults: about 4 waves of 2 fused blocks / 8 waves of 6 split
@@ -460,9 +463,10 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
   const int tiles_s = ((n[0] + 31) / 32) * ((n[1] + 7) / 8);
   const int zf = std::max(2, std::min(64, n[2] * tiles_f / 1216));
   const int zs = std::max(2, std::min(32, n[2] * tiles_s / 7296));
+  const int zt = std::max(4, std::min(64, n[2] * tiles_s / 1216));
   if (ctx->pd_form) {
-    form = ctx->pd_form;
-    zchunk = ctx->pd_zchunk ? ctx->pd_zchunk : (form == 1 ? zf : zs);
+    form = ctx->pd_form == 3 && !tma ? 2 : ctx->pd_form;
+    zchunk = ctx->pd_zchunk ? ctx->pd_zchunk : (form == 1 ? zf : form == 2 ? zs : zt);
     return WAP_OK;
   }
   auto it = ctx->pd_plans.find(key);
@@ -476,6 +480,9 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
     if (z >= 1 && z <= n[2]) cand.emplace_back(1, z);
   for (int z : {zs / 2, zs, zs * 2, zs * 4})
     if (z >= 1 && z <= n[2]) cand.emplace_back(2, z);
+  if (tma)
+    for (int z : {zt / 2, zt, zt * 2})
+      if (z >= 2 && z <= n[2]) cand.emplace_back(3, z);
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
@@ -568,7 +575,24 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   TRY(proven(((uint64_t)1 << 32) | den_bits, fastdiv));
   TRY(proven(0, rcp));
   int form = 0, zchunk = 0;
+  if (w->tma_state == 0) {
+    w->tma_state = -1;
+    if (pd_tma_supported(D) && w->tma_err.ensure(sizeof(int)) == cudaSuccess &&
+        make_pd_tma_maps(D, w->y.as<float>(), w->u.as<float>(), w->va.as<float>(), &w->ymap[0], &w->umap,
+                         &w->vmap[0]) == cudaSuccess &&
+        make_pd_tma_maps(D, w->y2.as<float>(), w->u.as<float>(), w->vb.as<float>(), &w->ymap[1], &w->umap,
+                         &w->vmap[1]) == cudaSuccess) {
+      w->tma_state = 1;
+      CU(cudaMemsetAsync(w->tma_err.p, 0, sizeof(int), ctx->stream));
+    }
+  }
   auto pd_launch = [&](int f, int zc, int mode, int store, int res) -> cudaError_t {
+    if (f == 3) {
+      const int yi = ycur == w->y.as<float>() ? 0 : 1, vi = vcur == w->va.as<float>() ? 0 : 1;
+      return launch_pd_tma(D, zc, &w->ymap[yi], &w->umap, &w->vmap[vi], ynext, w->u.as<float>(), vnext,
+                           w->kty.as<float>(), w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp,
+                           store, res, acc, w->tma_err.as<int>(), ctx->stream);
+    }
     if (f == 1)
       return launch_pd_fused(D, zc, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
                              w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp, store, res, acc,
@@ -586,7 +610,15 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream));
     ctx->stats.advect_voxels += (double)nv;
     KL(launch_linearize(D, w->warp.as<float>(), I1, vcur, w->u.as<float>(), w->kx4prev.as<float>(), ctx->stream));
-    if (wi == 0 && max_iters >= 0) TRY(pd_plan(ctx, D, pd_launch, form, zchunk));
+    if (wi == 0 && max_iters >= 0) {
+      TRY(pd_plan(ctx, D, pd_launch, form, zchunk, w->tma_state == 1));
+      if (w->tma_state == 1) {  // a tuning launch of the TMA form must not have timed out either
+        int bad = 0;
+        CU(cudaMemcpyAsync(&bad, w->tma_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        CU(cudaStreamSynchronize(ctx->stream));
+        CHECK(bad == 0, WAP_ECUDA, "primal-dual TMA pipeline: a barrier wait timed out");
+      }
+    }
     int it = 0;
     float err = 1.0f;
     // Profile only the largest grid seen in this outer iteration.
@@ -628,6 +660,12 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     if (pending) {
       CU(cudaStreamSynchronize(ctx->stream));
       TRY(drain());
+    }
+    if (form == 3) {
+      int bad = 0;
+      CU(cudaMemcpyAsync(&bad, w->tma_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      CU(cudaStreamSynchronize(ctx->stream));
+      CHECK(bad == 0, WAP_ECUDA, "primal-dual TMA pipeline: a barrier wait timed out");
     }
     ctx->stats.pd_voxel_iters += (double)it * (double)nv;
     if (iters_out) iters_out[wi] = it;
@@ -952,7 +990,7 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
   CHECK(ctx && key, WAP_EINVAL, "null argument");
   const std::string k = key;
   if (k == "pd_form") {
-    CHECK(value >= 0 && value <= 2, WAP_EINVAL, "pd_form must be 0, 1 or 2");
+    CHECK(value >= 0 && value <= 3, WAP_EINVAL, "pd_form must be 0, 1, 2 or 3");
     ctx->pd_form = value;
   } else if (k == "pd_zchunk") {
     CHECK(value >= 0, WAP_EINVAL, "pd_zchunk must be >= 0");

@@ -45,6 +45,19 @@ cudaError_t launch_pd_split(const FlowDims &D, int zchunk, const float *yin, flo
                             const float *vin, float *vout, float *kty, const float *kx4prev, int kxold_mode,
                             float lambda, float sigma1, float rinv, int fastdiv, int rcp, int store_kty,
                             int residual, double *acc, cudaStream_t st);
+// The TMA-fed fused form (nx % 4 == 0).  Tensor maps (64-byte opaque
+// descriptors, 64-byte aligned storage) over y (10 ch), u (4 ch), v (3 ch).
+struct alignas(64) PdTmaMap {
+  unsigned char bytes[128];
+};
+bool pd_tma_supported(const FlowDims &D);
+int pd_tma_smem_bytes();
+cudaError_t make_pd_tma_maps(const FlowDims &D, const float *y, const float *u, const float *v, void *ymap,
+                             void *umap, void *vmap);
+cudaError_t launch_pd_tma(const FlowDims &D, int zchunk, const void *ymap, const void *umap, const void *vmap,
+                          float *yout, const float *u, float *vout, float *kty, const float *kx4prev, int kxold_mode,
+                          float lambda, float sigma1, float rinv, int fastdiv, int rcp, int store_kty, int residual,
+                          double *acc, int *err, cudaStream_t st);
 // Counts the float inputs for which the FMA-corrected division by den differs
 // from IEEE division (0 proves the fast path exact for this den).
 cudaError_t launch_pd_fastdiv_check(float den, float rinv, unsigned long long *d_bad, cudaStream_t st);

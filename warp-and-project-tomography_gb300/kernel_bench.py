@@ -1,7 +1,7 @@
 """Per-kernel micro-benchmark of the GB300 library (device-resident inputs,
 CUDA-event timing on the library's stream).
 
-    python kernel_bench.py --kernel pd --n 256 --iters 100
+    python kernel_bench.py --kernel pd --n 256 --iters 100 [--pd-form 0|1|2|3]
     python kernel_bench.py --kernel fp|bp|bp_exact|advect|all --n 256 --det 384
 
 Prints one JSON line per kernel: milliseconds per launch and the achieved
@@ -35,6 +35,8 @@ def main():
     ap.add_argument("--det", type=int, default=384)
     ap.add_argument("--iters", type=int, default=20)
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--pd-form", type=int, default=0, help="0 autotuned, 1 fused, 2 primal+dual, 3 TMA-fed fused")
+    ap.add_argument("--pd-zchunk", type=int, default=0)
     a = ap.parse_args()
     build.build()
     n, d = a.n, a.det
@@ -101,10 +103,13 @@ def main():
         V = torch.randn((3, n, n, n), device="cuda", generator=g)
         Y = [torch.zeros((3, n, n, n), device="cuda") for _ in range(3)] + [torch.zeros((n, n, n), device="cuda")]
         ctx.set_profiling(True)
+        ctx.set_tuning("pd_form", a.pd_form)
+        ctx.set_tuning("pd_zchunk", a.pd_zchunk)
         its = ctx.flow_level([n, n, n], I1, I2, V, *Y, 0.0, 0.05, a.iters - 1, 1, [0, n, 0, n, 0, n], [8] * 6)
         st = ctx.stats()
         ms = st.ms_pd / max(st.pd_timed, 1)
-        report("pd", ms, 120 * nv, {"iterations": int(its[0])})
+        form, zc = ctx.get_tuning([n, n, n])
+        report("pd", ms, 120 * nv, {"iterations": int(its[0]), "form": form, "zchunk": zc})
     ctx.close()
 
 
