@@ -74,6 +74,8 @@ def parse():
                     help="jobs of the served-form measurement added to the line (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-workers", type=int, default=3)
+    ap.add_argument("--batch-jobs", type=int, default=12,
+                    help="scans of the batched-form comparison added to the line (0: skip)")
     return ap.parse_args()
 
 
@@ -363,15 +365,21 @@ def run_gb300(args):
         sec, parts, sample = cpu_sample(args, counts, threads)
         result["cpu_baseline"] = {"value": 1.0 / sec, "unit": "outer-iter/s", "cores": threads, "kind": "port",
                                   "sample": sample, "component_seconds": parts}
+    if rank == 0 and world == 1 and (args.serve_jobs > 0 or args.batch_jobs > 0):
+        del projs
+        ctx.close()
+        torch.cuda.empty_cache()
     if rank == 0 and world == 1 and args.serve_jobs > 0:
         # Served form: p50/p95/p99 latency of a Poisson job stream through the
         # request loop (see serving.py for the job mix).
         import serving
-        del projs
-        ctx.close()
-        torch.cuda.empty_cache()
         result["serving"] = serving.run(wap, torch, n_jobs=args.serve_jobs, rate=args.serve_rate,
                                         workers=args.serve_workers)
+    if rank == 0 and world == 1 and args.batch_jobs > 0:
+        # Batched form: uneven scans looped through the plain path vs overlapped
+        # through the request loop (same results, checked).
+        import serving
+        result["batched"] = serving.run_batched(wap, torch, n_jobs=args.batch_jobs)
     if rank == 0:
         print(json.dumps(result))
     if dist:
