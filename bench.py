@@ -295,6 +295,8 @@ def run_gb300(args):
                kernel_launches=0, flow_pd_iterations=0, ms_pd=0.0, pd_timed=0, ms_cp=0.0, ms_flow=0.0, ms_wap=0.0)
     h2d_bytes = 0
     pd_vox = 0
+    lev_ms = [0.0] * args.scales
+    lev_its = [0] * args.scales
     for i in range(args.warmup, args.warmup + args.steps):
         f = order[i]
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
@@ -314,6 +316,9 @@ def run_gb300(args):
         h2d_bytes += (s1 - s0) * np_ * 4
         for k in agg:
             agg[k] += getattr(s, k)
+        for l in range(args.scales):
+            lev_ms[l] += s.ms_flow_level[l]
+            lev_its[l] += s.pd_iters_level[l]
         pd_vox = max(pd_vox, s.pd_timed_voxels)
     torch.cuda.synchronize()
     clk = clocks.stop()
@@ -353,6 +358,9 @@ def run_gb300(args):
                      "ms_per_launch": pd_ms, "launches_timed": int(agg["pd_timed"])},
         "phase_ms_per_step": {"cp_sart": agg["ms_cp"] / K, "flow": agg["ms_flow"] / K, "wap": agg["ms_wap"] / K},
         "pd_iterations_per_step": agg["flow_pd_iterations"] / K,
+        "flow_levels_finest_first": {"sides": [int(n * 0.5 ** l) for l in range(args.scales)],
+                                     "ms_per_step": [v / K for v in lev_ms],
+                                     "pd_iterations_per_step": [v / K for v in lev_its]},
         "op_counts_per_outer_iteration": {k: agg[k] * F / K for k in ("projections", "backprojections",
                                                                        "advect_voxels", "cp_frame_passes",
                                                                        "pd_voxel_iters")},

@@ -85,6 +85,11 @@ typedef struct {
   double ms_pd;                  /* profiled: device time of the PD iterations at the largest grid */
   long long pd_timed;            /* profiled: PD iterations in ms_pd */
   long long pd_timed_voxels;     /* profiled: voxels of that grid */
+  /* per flow pyramid level, index 0 = finest: device time of the level's
+   * solve (warps, linearisations, primal-dual iterations) and its
+   * primal-dual iterations, summed over the pairs */
+  double ms_flow_level[8];
+  long long pd_iters_level[8];
 } wap_stats;
 
 /* ---- context ---------------------------------------------------------- */

@@ -732,14 +732,22 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
     }
   }
   const float aabb[6] = {0, (float)dims[0], 0, (float)dims[1], 0, (float)dims[2]};
+  std::vector<cudaEvent_t> lev(scales + 1);
+  for (auto &e : lev) CU(cudaEventCreate(&e));
+  CU(cudaEventRecord(lev[0], ctx->stream));
   for (int l = 0; l < scales; ++l) {
     PyramidLevel &P = *ctx->pyramid[l];
     const size_t m = (size_t)P.d[0] * P.d[1] * P.d[2];
     int roi[6];
     for (int i = 0; i < 6; ++i) roi[i] = (float)cut6[i] * ((float)P.d[i / 2] / (float)dims[i / 2]);
     float *Y[4] = {P.y.as<float>(), P.y.as<float>() + 3 * m, P.y.as<float>() + 6 * m, P.y.as<float>() + 9 * m};
+    long long before = total ? *total : 0, its = 0;
     TRY(flow_level(ctx, P.d, P.i1.as<float>(), P.i2.as<float>(), P.v.as<float>(), Y, tol, lambda, max_iters, nwarps,
-                   aabb, roi, nullptr, total));
+                   aabb, roi, nullptr, &its));
+    if (total) *total = before + its;
+    const int fine_idx = scales - 1 - l;  // 0 = finest
+    if (fine_idx < 8) ctx->stats.pd_iters_level[fine_idx] += its;
+    CU(cudaEventRecord(lev[l + 1], ctx->stream));
     if (l + 1 < scales) {
       PyramidLevel &N = *ctx->pyramid[l + 1];
       TRY(do_resize(ctx, P.d, 3, P.v.as<float>(), N.d, N.v.as<float>()));
@@ -748,6 +756,12 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
   }
   CU(cudaMemcpyAsync(Vout, fine.v.p, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));  // b1/b2 are released on return
+  for (int l = 0; l < scales; ++l) {
+    float ms = 0.0f;
+    CU(cudaEventElapsedTime(&ms, lev[l], lev[l + 1]));
+    if (scales - 1 - l < 8) ctx->stats.ms_flow_level[scales - 1 - l] += ms;
+  }
+  for (auto &e : lev) cudaEventDestroy(e);
   return WAP_OK;
 }
 

@@ -70,6 +70,8 @@ class Stats(ctypes.Structure):
         ("ms_pd", _c_double),
         ("pd_timed", ctypes.c_longlong),
         ("pd_timed_voxels", ctypes.c_longlong),
+        ("ms_flow_level", _c_double * 8),
+        ("pd_iters_level", ctypes.c_longlong * 8),
     ]
 
 
