@@ -54,7 +54,7 @@ PD_BYTES_MIN_PER_VOXEL = 4 * (10 + 10 + 3 + 3 + 4)
 # DRAM bytes (read + write) of one primal-dual iteration at 256^3 per kernel
 # form (1 fused, 2 primal + dual, 3 TMA-fed fused), from ncu captures (dram__bytes_read.sum +
 # dram__bytes_write.sum) of kernel_bench.py.
-PD_TRAFFIC_256 = {1: 1.98e9, 2: 3.29e9, 3: None}
+PD_TRAFFIC_256 = {1: 1.98e9, 2: 3.29e9, 3: 1.98e9}
 PD_FORMS = {1: "pd_fused_kernel", 2: "pd_primal_kernel + pd_dual_kernel", 3: "pd_tma_kernel (TMA-fed fused)"}
 
 

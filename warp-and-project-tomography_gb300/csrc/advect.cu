@@ -8,6 +8,7 @@
 // FP32 without contraction so the result matches the reference bit for bit.
 // The world position of each cell centre involves a double division in the
 // reference (cell_grid_to_world); it is tabulated per axis on the host.
+#include <algorithm>
 #include <vector>
 
 #include "wap_internal.h"
@@ -169,9 +170,17 @@ cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d
     G.a1[a] = aabb[2 * a + 1];
   }
   const dim3 block(32, 4, 1);
-  const dim3 grid((dims[0] + 31) / 32, (dims[1] + 3) / 4, dims[2] * njobs);
-  advect_kernel<<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1], d_jobs, nc);
-  return cudaGetLastError();
+  // jobs x z planes go in gridDim.z; more than 65535 are split into launches
+  // of whole jobs
+  const int per = std::max(1, 65535 / dims[2]);
+  for (int j = 0; j < njobs; j += per) {
+    const int n = std::min(per, njobs - j);
+    const dim3 grid((dims[0] + 31) / 32, (dims[1] + 3) / 4, dims[2] * n);
+    advect_kernel<<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1], d_jobs + j, nc);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st) {

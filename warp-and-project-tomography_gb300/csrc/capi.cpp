@@ -515,6 +515,9 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
 int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2, float *V, float *Y[4], float tol,
                float lambda, int max_iters, int nwarps, const float aabb[6], const int roi6[6], int *iters_out,
                long long *total) {
+  // The primal-dual kernels index the 10-component dual with 32-bit offsets.
+  CHECK(10ull * dims[0] * dims[1] * dims[2] < (1ull << 32), WAP_ETOOBIG,
+        "flow grid too large for 32-bit offsets (under 2^32/10 voxels)");
   FlowWork *w = flow_work(ctx, dims);
   CHECK(w, WAP_ENOMEM, "flow workspace allocation failed");
   const size_t nv = (size_t)dims[0] * dims[1] * dims[2];

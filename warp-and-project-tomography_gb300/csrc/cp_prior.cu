@@ -8,6 +8,8 @@
 // the (frame-parallel) SART sweeps: dual(all) -> primal(all) -> SART(all) ->
 // over-relaxation(all).  Only channel 0 of the reference's 3-channel Y_tp /
 // X_bar is ever read and Y_bc stays zero, so they are one channel here.
+#include <algorithm>
+
 #include "wap_flow.h"
 
 namespace wap {
@@ -88,26 +90,47 @@ __global__ void cp_overrelax_kernel(CpArgs a, const float *__restrict__ vol, con
 
 }  // namespace
 
+// The frames of a batch go in gridDim.z (z planes x frames); batches whose
+// product would pass 65535 are split into several launches of whole frames.
+// Each stage (dual, primal, over-relaxation) only reads what the previous
+// stage wrote, so splitting a stage changes nothing.
+template <class Launch>
+cudaError_t for_frame_chunks(const CpArgs &a, int zplanes, Launch launch) {
+  const int per = std::max(1, 65535 / std::max(1, zplanes));
+  for (int f = 0; f < a.F; f += per) {
+    CpArgs c = a;
+    c.f0 = a.f0 + f;
+    c.F = std::min(per, a.F - f);
+    launch(c);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t launch_cp_dual(const CpArgs &a, const float *xbar, const float *xbar_zero, float *ytv, float *ytp,
                            cudaStream_t st) {
-  const dim3 b(32, 8, 1), g((a.n[0] + 31) / 32, (a.n[1] + 7) / 8, a.n[2] * a.F);
-  cp_dual_kernel<<<g, b, 0, st>>>(a, xbar, xbar_zero, ytv, ytp);
-  return cudaGetLastError();
+  return for_frame_chunks(a, a.n[2], [&](const CpArgs &c) {
+    const dim3 b(32, 8, 1), g((c.n[0] + 31) / 32, (c.n[1] + 7) / 8, c.n[2] * c.F);
+    cp_dual_kernel<<<g, b, 0, st>>>(c, xbar, xbar_zero, ytv, ytp);
+  });
 }
 
 cudaError_t launch_cp_primal(const CpArgs &a, const float *ytp, const float *ytv, float *vol, float *xprev,
                              cudaStream_t st) {
-  const dim3 b(32, 8, 1), g((a.n[0] + 31) / 32, (a.n[1] + 7) / 8, a.n[2] * a.F);
-  cp_primal_kernel<<<g, b, 0, st>>>(a, ytp, ytv, vol, xprev);
-  return cudaGetLastError();
+  return for_frame_chunks(a, a.n[2], [&](const CpArgs &c) {
+    const dim3 b(32, 8, 1), g((c.n[0] + 31) / 32, (c.n[1] + 7) / 8, c.n[2] * c.F);
+    cp_primal_kernel<<<g, b, 0, st>>>(c, ytp, ytv, vol, xprev);
+  });
 }
 
 cudaError_t launch_cp_overrelax(const CpArgs &a, const float *vol, const float *xprev, float *xbar, cudaStream_t st) {
   const int bx = a.box[1] - a.box[0], by = a.box[3] - a.box[2], bz = a.box[5] - a.box[4];
   if (bx <= 0 || by <= 0 || bz <= 0) return cudaSuccess;
-  const dim3 b(32, 8, 1), g((bx + 31) / 32, (by + 7) / 8, bz * a.F);
-  cp_overrelax_kernel<<<g, b, 0, st>>>(a, vol, xprev, xbar);
-  return cudaGetLastError();
+  return for_frame_chunks(a, bz, [&](const CpArgs &c) {
+    const dim3 b(32, 8, 1), g((bx + 31) / 32, (by + 7) / 8, bz * c.F);
+    cp_overrelax_kernel<<<g, b, 0, st>>>(c, vol, xprev, xbar);
+  });
 }
 
 }  // namespace wap
