@@ -77,22 +77,30 @@ __device__ __forceinline__ float sample(const float *__restrict__ img, const Gri
     mn = std_min(mn, v);
     mx = std_max(mx, v);
   }
-  float planes[4];
-#pragma unroll
+  // One z plane of 16 taps per loop trip (not unrolled): the loads in flight
+  // stay at 16 per thread, which keeps the register count low enough for
+  // several blocks per SM; the arithmetic and its order are unchanged.
+  float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, p3 = 0.0f;
+#pragma unroll 1
   for (int kz = 0; kz < 4; ++kz) {
+    const int z = kz == 0 ? s.zs[0] : kz == 1 ? s.zs[1] : kz == 2 ? s.zs[2] : s.zs[3];
     float rows[4];
 #pragma unroll
     for (int ky = 0; ky < 4; ++ky) {
-      const int y = s.ys[ky], z = s.zs[kz];
+      const int y = s.ys[ky];
       rows[ky] = cubf(I(s.xs[0], y, z), I(s.xs[1], y, z), I(s.xs[2], y, z), I(s.xs[3], y, z), s.dx);
     }
-    planes[kz] = cubf(rows[0], rows[1], rows[2], rows[3], s.dy);
+    const float pl = cubf(rows[0], rows[1], rows[2], rows[3], s.dy);
+    p0 = kz == 0 ? pl : p0;
+    p1 = kz == 1 ? pl : p1;
+    p2 = kz == 2 ? pl : p2;
+    p3 = kz == 3 ? pl : p3;
   }
-  const float c = cubf(planes[0], planes[1], planes[2], planes[3], s.dz);
+  const float c = cubf(p0, p1, p2, p3, s.dz);
   return std_max(mn, std_min(mx, c));
 }
 
-__global__ void __launch_bounds__(128) advect_kernel(Grid3 G, const float *__restrict__ wx,
+__global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__restrict__ wx,
                                                      const float *__restrict__ wy, const float *__restrict__ wz,
                                                      const AdvectJob *__restrict__ jobs, int nc) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
