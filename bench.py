@@ -74,6 +74,10 @@ def parse():
                     help="jobs of the served-form measurement added to the line (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=20.0)
     ap.add_argument("--serve-workers", type=int, default=3)
+    ap.add_argument("--flow-bits", type=int, default=32, choices=[32, 16],
+                    help="32: the reference's arithmetic; 16: the precision form (FP16 flow state)")
+    ap.add_argument("--precision-steps", type=int, default=2,
+                    help="frame-steps re-timed in the precision form for the line's precision_form object (0: skip)")
     ap.add_argument("--batch-jobs", type=int, default=12,
                     help="scans of the batched-form comparison added to the line (0: skip)")
     return ap.parse_args()
@@ -253,6 +257,7 @@ def run_gb300(args):
         ctx, projs, ang, meta = workload(args, torch, factory)
     F = meta["nframes"]
     ctx.set_projections_device(projs)
+    ctx.set_tuning("flow_bits", args.flow_bits)
     ctx.level_setup(0)
     sched = wap.reference_schedule(n_cp=5, nb_sart=2, wp_frames=F, flow_iters=args.flow_iters,
                                    flow_scales=args.scales, flow_tol=0.008, cut=8, bp_exact=1)
@@ -328,6 +333,27 @@ def run_gb300(args):
         tdist.barrier()
     K = args.steps
     value = replicas.aggregate_rate(world, K / F, t_dev)
+    precision = None
+    if world == 1 and args.precision_steps > 0 and args.flow_bits == 32:
+        # The same frame-steps again with the flow solver's state in FP16.
+        ctx.set_tuning("flow_bits", 16)
+        t16 = 0.0
+        for i in range(args.warmup, args.warmup + args.precision_steps):
+            f = order[args.warmup + (i - args.warmup) % args.steps]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+            ctx.outer_iteration_frames(sched, f, f + 1)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            stream.synchronize()
+            t16 += e0.elapsed_time(e1) / 1e3
+        ctx.set_tuning("flow_bits", 32)
+        v16 = replicas.aggregate_rate(1, args.precision_steps / F, t16)
+        precision = {"flow_bits": 16, "value": v16, "unit": "outer-iter/s", "ms_per_step": t16 / args.precision_steps * 1e3,
+                     "speedup_vs_fp32": v16 / value,
+                     "note": "the timed frames re-run with the flow solver's dual, flow and linearisation stored in "
+                             "FP16 (FP32 arithmetic); accuracy: tests/test_gpu_parity.py::test_precision_form_*"}
     e2e = replicas.aggregate_rate(world, K / F, t_e2e)
     pd_ms = agg["ms_pd"] / max(agg["pd_timed"], 1)
     achieved = PD_BYTES_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9
@@ -366,6 +392,10 @@ def run_gb300(args):
                                                                        "pd_voxel_iters")},
         "clocks": clk,
     }
+    if precision:
+        result["precision_form"] = precision
+    if args.flow_bits == 16:
+        result["dtype"] = "f32 arithmetic, f16 flow state"
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         counts = {k: agg[k] * F / K for k in ("projections", "backprojections", "advect_voxels", "cp_frame_passes",
                                                "pd_voxel_iters")}

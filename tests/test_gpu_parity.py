@@ -234,7 +234,7 @@ def test_flow_level_autotuned_plan(setup):
     aabb = np.array([0, dims[0], 0, dims[1], 0, dims[2]], np.float32)
     ctx.flow_level(list(dims), dev(torch, I1), dev(torch, I2), V, *Y, 0.0, 0.05, 10, 1, aabb, [2] * 6)
     form, zchunk = ctx.get_tuning(list(dims))
-    assert form in (1, 2) and 1 <= zchunk <= dims[2]
+    assert form in (1, 2, 3) and 1 <= zchunk <= dims[2]
 
 
 def test_flow_multiscale_bitexact(setup, orc):
@@ -345,3 +345,41 @@ def test_cg_screened_laplacian(setup, orc, mode):
     it = ctx.cg_screened_laplacian([N] * 3, 1.0, 0.5, dev(torch, rhs), dx, 1e-5, 200, 1e-9, mode)
     assert abs(it - oit) <= 2
     assert rel_l2(host(dx), xo) < 1e-4
+
+
+def test_precision_form_fp16_flow_state(setup, orc, wapmod):
+    """The precision form (flow solver state in FP16, FP32 arithmetic): same
+    iteration counts at a fixed count, the flow within the stated tolerance of
+    the FP32 path, and an outer iteration's volumes within 1e-3 relative L2 of
+    the oracle."""
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    aabb, I1, I2 = _flow_inputs(s, orc)
+    V0 = (s["flow"] * 0.3).astype(np.float32)
+    out = {}
+    try:
+        for bits in (32, 16):
+            ctx.set_tuning("flow_bits", bits)
+            dV = dev(torch, V0)
+            dY = [torch.zeros((3, N, N, N), device="cuda") for _ in range(3)] + [torch.zeros((N, N, N), device="cuda")]
+            its = ctx.flow_level([N] * 3, dev(torch, I1), dev(torch, I2), dV, *dY, 0.0, 0.05, 200, 2, aabb, [4] * 6)
+            out[bits] = (host(dV), list(its))
+        assert out[16][1] == out[32][1]
+        assert rel_l2(out[16][0], out[32][0]) < 2e-2
+        # an outer iteration with the precision form against the FP32 oracle
+        import oracle as O
+        F = ctx.level_setup(0)
+        sched_w = wapmod.reference_schedule(n_cp=2, nb_sart=2, wp_frames=2, flow_iters=60, flow_scales=2,
+                                            flow_tol=0.0, flow_warps=2)
+        ctx.outer_iteration(sched_w)
+        sched_o = O.Schedule(n_cp=2, nb_sart=2, nb_projwarp=1, wp_frames=2, flow_tol=0.0, flow_lambda=0.05,
+                             flow_iters=60, flow_warps=2, flow_eta=0.5, flow_sigma=0.8, flow_scales=2, cut=8,
+                             deterministic=1)
+        state = dict(vols=np.zeros((F, N, N, N), np.float32), flows=np.zeros((F, 3, N, N, N), np.float32),
+                     ytv=np.zeros((F, 3, N, N, N), np.float32), ytp=np.zeros((F, N, N, N), np.float32),
+                     xbar=np.zeros((F, N, N, N), np.float32), xprev=np.zeros((F, N, N, N), np.float32))
+        orc.outer_iteration(s["oscan"], sched_o, s["ang"], s["projs"], 0, state)
+        for f in range(F):
+            assert rel_l2(ctx.download_volume(f), state["vols"][f]) < 1e-3
+    finally:
+        ctx.set_tuning("flow_bits", 32)

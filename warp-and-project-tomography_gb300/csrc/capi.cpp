@@ -73,6 +73,10 @@ struct FlowWork {
   // Tensor maps of the TMA-fed form: y over (y, y2), v over (va, vb), u.
   int tma_state = 0;  // 0: not made, 1: made, -1: unavailable for this grid
   PdTmaMap ymap[2], vmap[2], umap;
+  // The precision form's FP16 copies of y, v, u and their tensor maps.
+  int h_state = 0;
+  DevMem yh[2], vh[2], uh;
+  PdTmaMap hymap[2], hvmap[2], humap;
 };
 
 // Multiscale pyramid buffers for one finest size.
@@ -122,7 +126,9 @@ struct wap_ctx {
   int profiling = 0;
   int pd_form = 0;    // 0: autotuned, 1: fused kernel, 2: primal + dual kernels
   int pd_zchunk = 0;  // 0: autotuned / default
+  int flow_bits = 32; // 16: the flow solver's y, v, u stored in FP16 (the precision form)
   std::map<std::tuple<int, int, int>, std::pair<int, int>> pd_plans;  // grid -> (form, zchunk)
+  std::map<std::tuple<int, int, int>, std::pair<int, int>> pd_plans16;  // the same for FP16 storage
   wap_observer_fn observer = nullptr;
   void *observer_user = nullptr;
   std::vector<cudaEvent_t> pd_events;  // pairs, reused per 50-iteration chunk
@@ -454,9 +460,10 @@ FlowWork *flow_work(wap_ctx *ctx, const int dims[3]) {
 // current iterate and writes the next-iterate buffers, which the real
 // iteration then overwrites, so tuning leaves the solver's state untouched.
 template <class Launch>
-int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zchunk, bool tma) {
+int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zchunk, bool tma, bool half = false) {
   const int *n = D.n;
   const auto key = std::make_tuple(n[0], n[1], n[2]);
+  auto &plans = half ? ctx->pd_plans16 : ctx->pd_plans;
   // z-chunk defaults: about 4 waves of 2 fused blocks / 8 waves of 6 split
   // blocks over the 152 SMs.
   const int tiles_f = ((n[0] + 31) / 32) * ((n[1] + 6) / 7);
@@ -464,25 +471,37 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
   const int zf = std::max(2, std::min(64, n[2] * tiles_f / 1216));
   const int zs = std::max(2, std::min(32, n[2] * tiles_s / 7296));
   const int zt = std::max(4, std::min(64, n[2] * tiles_s / 1216));
-  if (ctx->pd_form) {
+  if (half) {  // FP16 storage exists only in the TMA form (form 4)
+    if (ctx->pd_zchunk) {
+      form = 4;
+      zchunk = ctx->pd_zchunk;
+      return WAP_OK;
+    }
+  } else if (ctx->pd_form) {
     form = ctx->pd_form == 3 && !tma ? 2 : ctx->pd_form;
     zchunk = ctx->pd_zchunk ? ctx->pd_zchunk : (form == 1 ? zf : form == 2 ? zs : zt);
     return WAP_OK;
   }
-  auto it = ctx->pd_plans.find(key);
-  if (it != ctx->pd_plans.end()) {
+  auto it = plans.find(key);
+  if (it != plans.end()) {
     form = it->second.first;
     zchunk = it->second.second;
     return WAP_OK;
   }
   std::vector<std::pair<int, int>> cand;
-  for (int z : {zf / 2, zf, zf * 2})
-    if (z >= 1 && z <= n[2]) cand.emplace_back(1, z);
-  for (int z : {zs / 2, zs, zs * 2, zs * 4})
-    if (z >= 1 && z <= n[2]) cand.emplace_back(2, z);
-  if (tma)
+  if (half) {
     for (int z : {zt / 2, zt, zt * 2})
-      if (z >= 2 && z <= n[2]) cand.emplace_back(3, z);
+      if (z >= 2 && z <= n[2]) cand.emplace_back(4, z);
+    if (cand.empty()) cand.emplace_back(4, std::max(1, n[2]));
+  } else {
+    for (int z : {zf / 2, zf, zf * 2})
+      if (z >= 1 && z <= n[2]) cand.emplace_back(1, z);
+    for (int z : {zs / 2, zs, zs * 2, zs * 4})
+      if (z >= 1 && z <= n[2]) cand.emplace_back(2, z);
+    if (tma)
+      for (int z : {zt / 2, zt, zt * 2})
+        if (z >= 2 && z <= n[2]) cand.emplace_back(3, z);
+  }
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
@@ -503,7 +522,7 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  ctx->pd_plans[key] = pick;
+  plans[key] = pick;
   form = pick.first;
   zchunk = pick.second;
   return WAP_OK;
@@ -580,22 +599,46 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   int form = 0, zchunk = 0;
   if (w->tma_state == 0) {
     w->tma_state = -1;
-    if (pd_tma_supported(D) && w->tma_err.ensure(sizeof(int)) == cudaSuccess &&
-        make_pd_tma_maps(D, w->y.as<float>(), w->u.as<float>(), w->va.as<float>(), &w->ymap[0], &w->umap,
-                         &w->vmap[0]) == cudaSuccess &&
-        make_pd_tma_maps(D, w->y2.as<float>(), w->u.as<float>(), w->vb.as<float>(), &w->ymap[1], &w->umap,
-                         &w->vmap[1]) == cudaSuccess) {
+    if (pd_tma_supported(D, false) && w->tma_err.ensure(sizeof(int)) == cudaSuccess &&
+        make_pd_tma_maps(D, false, w->y.p, w->u.p, w->va.p, &w->ymap[0], &w->umap, &w->vmap[0]) == cudaSuccess &&
+        make_pd_tma_maps(D, false, w->y2.p, w->u.p, w->vb.p, &w->ymap[1], &w->umap, &w->vmap[1]) == cudaSuccess) {
       w->tma_state = 1;
       CU(cudaMemsetAsync(w->tma_err.p, 0, sizeof(int), ctx->stream));
     }
   }
-  auto pd_launch = [&](int f, int zc, int mode, int store, int res) -> cudaError_t {
-    if (f == 3) {
-      const int yi = ycur == w->y.as<float>() ? 0 : 1, vi = vcur == w->va.as<float>() ? 0 : 1;
-      return launch_pd_tma(D, zc, &w->ymap[yi], &w->umap, &w->vmap[vi], ynext, w->u.as<float>(), vnext,
-                           w->kty.as<float>(), w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp,
-                           store, res, acc, w->tma_err.as<int>(), ctx->stream);
+  // The precision form: y, v, u live in FP16 copies during the iterations
+  // (FP32 arithmetic); the FP32 buffers are refreshed where the rest of the
+  // solver reads them (before each warp's advection and at the end).
+  if (ctx->flow_bits == 16 && w->h_state == 0) {
+    w->h_state = -1;
+    if (pd_tma_supported(D, true) && w->tma_err.ensure(sizeof(int)) == cudaSuccess &&
+        w->yh[0].ensure(2 * 10 * nv) == cudaSuccess && w->yh[1].ensure(2 * 10 * nv) == cudaSuccess &&
+        w->vh[0].ensure(2 * 3 * nv) == cudaSuccess && w->vh[1].ensure(2 * 3 * nv) == cudaSuccess &&
+        w->uh.ensure(2 * 4 * nv) == cudaSuccess &&
+        make_pd_tma_maps(D, true, w->yh[0].p, w->uh.p, w->vh[0].p, &w->hymap[0], &w->humap, &w->hvmap[0]) ==
+            cudaSuccess &&
+        make_pd_tma_maps(D, true, w->yh[1].p, w->uh.p, w->vh[1].p, &w->hymap[1], &w->humap, &w->hvmap[1]) ==
+            cudaSuccess) {
+      w->h_state = 1;
+      CU(cudaMemsetAsync(w->tma_err.p, 0, sizeof(int), ctx->stream));
     }
+  }
+  const bool half = ctx->flow_bits == 16 && w->h_state == 1;
+  if (half) {
+    KL(launch_to_half(10 * nv, y, w->yh[0].p, ctx->stream));
+    KL(launch_to_half(3 * nv, w->va.as<float>(), w->vh[0].p, ctx->stream));
+    KL(launch_to_half(3 * nv, w->vb.as<float>(), w->vh[1].p, ctx->stream));
+  }
+  auto pd_launch = [&](int f, int zc, int mode, int store, int res) -> cudaError_t {
+    const int yi = ycur == w->y.as<float>() ? 0 : 1, vi = vcur == w->va.as<float>() ? 0 : 1;
+    if (f == 4)
+      return launch_pd_tma(D, zc, true, &w->hymap[yi], &w->humap, &w->hvmap[vi], w->yh[1 - yi].p,
+                           w->vh[1 - vi].p, w->kty.as<float>(), w->kx4prev.as<float>(), mode, lambda, sigma1, rinv,
+                           fastdiv, rcp, store, res, acc, w->tma_err.as<int>(), ctx->stream);
+    if (f == 3)
+      return launch_pd_tma(D, zc, false, &w->ymap[yi], &w->umap, &w->vmap[vi], ynext, vnext, w->kty.as<float>(),
+                           w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp, store, res, acc,
+                           w->tma_err.as<int>(), ctx->stream);
     if (f == 1)
       return launch_pd_fused(D, zc, ycur, ynext, w->u.as<float>(), vcur, vnext, w->kty.as<float>(),
                              w->kx4prev.as<float>(), mode, lambda, sigma1, rinv, fastdiv, rcp, store, res, acc,
@@ -613,9 +656,10 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream));
     ctx->stats.advect_voxels += (double)nv;
     KL(launch_linearize(D, w->warp.as<float>(), I1, vcur, w->u.as<float>(), w->kx4prev.as<float>(), ctx->stream));
+    if (half) KL(launch_to_half(4 * nv, w->u.as<float>(), w->uh.p, ctx->stream));
     if (wi == 0 && max_iters >= 0) {
-      TRY(pd_plan(ctx, D, pd_launch, form, zchunk, w->tma_state == 1));
-      if (w->tma_state == 1) {  // a tuning launch of the TMA form must not have timed out either
+      TRY(pd_plan(ctx, D, pd_launch, form, zchunk, w->tma_state == 1, half));
+      if (w->tma_state == 1 || half) {  // a tuning launch of the TMA form must not have timed out either
         int bad = 0;
         CU(cudaMemcpyAsync(&bad, w->tma_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
         CU(cudaStreamSynchronize(ctx->stream));
@@ -664,7 +708,8 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
       CU(cudaStreamSynchronize(ctx->stream));
       TRY(drain());
     }
-    if (form == 3) {
+    if (half) KL(launch_from_half(3 * nv, w->vh[vcur == w->va.as<float>() ? 0 : 1].p, vcur, ctx->stream));
+    if (form >= 3) {
       int bad = 0;
       CU(cudaMemcpyAsync(&bad, w->tma_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
       CU(cudaStreamSynchronize(ctx->stream));
@@ -675,6 +720,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     if (total) *total += it;
     ctx->stats.flow_pd_iterations += it;
   }
+  if (half) KL(launch_from_half(10 * nv, w->yh[ycur == w->y.as<float>() ? 0 : 1].p, ycur, ctx->stream));
   CU(cudaMemcpyAsync(V, vcur, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
   for (int q = 0; q < 3; ++q) KL(launch_roi_copy(D, 3, ycur + 3 * q * nv, Y[q], ctx->stream));
   KL(launch_roi_copy(D, 1, ycur + 9 * nv, Y[3], ctx->stream));
@@ -1009,6 +1055,9 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
   if (k == "pd_form") {
     CHECK(value >= 0 && value <= 3, WAP_EINVAL, "pd_form must be 0, 1, 2 or 3");
     ctx->pd_form = value;
+  } else if (k == "flow_bits") {
+    CHECK(value == 32 || value == 16, WAP_EINVAL, "flow_bits must be 32 or 16");
+    ctx->flow_bits = value;
   } else if (k == "pd_zchunk") {
     CHECK(value >= 0, WAP_EINVAL, "pd_zchunk must be >= 0");
     ctx->pd_zchunk = value;
@@ -1016,6 +1065,7 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
     return fail(ctx, WAP_EINVAL, "unknown tuning key: " + k);
   }
   ctx->pd_plans.clear();
+  ctx->pd_plans16.clear();
   return WAP_OK;
 }
 

@@ -50,14 +50,18 @@ cudaError_t launch_pd_split(const FlowDims &D, int zchunk, const float *yin, flo
 struct alignas(64) PdTmaMap {
   unsigned char bytes[128];
 };
-bool pd_tma_supported(const FlowDims &D);
-int pd_tma_smem_bytes();
-cudaError_t make_pd_tma_maps(const FlowDims &D, const float *y, const float *u, const float *v, void *ymap,
+// half = the precision form: y, u, v stored in FP16 (nx % 8 == 0), FP32
+// arithmetic; otherwise FP32 storage (nx % 4 == 0).
+bool pd_tma_supported(const FlowDims &D, bool half);
+cudaError_t make_pd_tma_maps(const FlowDims &D, bool half, const void *y, const void *u, const void *v, void *ymap,
                              void *umap, void *vmap);
-cudaError_t launch_pd_tma(const FlowDims &D, int zchunk, const void *ymap, const void *umap, const void *vmap,
-                          float *yout, const float *u, float *vout, float *kty, const float *kx4prev, int kxold_mode,
+cudaError_t launch_pd_tma(const FlowDims &D, int zchunk, bool half, const void *ymap, const void *umap,
+                          const void *vmap, void *yout, void *vout, float *kty, const float *kx4prev, int kxold_mode,
                           float lambda, float sigma1, float rinv, int fastdiv, int rcp, int store_kty, int residual,
                           double *acc, int *err, cudaStream_t st);
+// FP32 <-> FP16 element conversion (round to nearest even).
+cudaError_t launch_to_half(size_t n, const float *src, void *dst, cudaStream_t st);
+cudaError_t launch_from_half(size_t n, const void *src, float *dst, cudaStream_t st);
 // Counts the float inputs for which the FMA-corrected division by den differs
 // from IEEE division (0 proves the fast path exact for this den).
 cudaError_t launch_pd_fastdiv_check(float den, float rinv, unsigned long long *d_bad, cudaStream_t st);

@@ -37,6 +37,7 @@ def main():
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--pd-form", type=int, default=0, help="0 autotuned, 1 fused, 2 primal+dual, 3 TMA-fed fused")
     ap.add_argument("--pd-zchunk", type=int, default=0)
+    ap.add_argument("--flow-bits", type=int, default=32, help="16: the precision form (FP16 flow state)")
     a = ap.parse_args()
     build.build()
     n, d = a.n, a.det
@@ -105,6 +106,7 @@ def main():
         ctx.set_profiling(True)
         ctx.set_tuning("pd_form", a.pd_form)
         ctx.set_tuning("pd_zchunk", a.pd_zchunk)
+        ctx.set_tuning("flow_bits", a.flow_bits)
         its = ctx.flow_level([n, n, n], I1, I2, V, *Y, 0.0, 0.05, a.iters - 1, 1, [0, n, 0, n, 0, n], [8] * 6)
         st = ctx.stats()
         ms = st.ms_pd / max(st.pd_timed, 1)
