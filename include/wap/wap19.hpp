@@ -448,6 +448,7 @@ class PSART {
     }
     m_RayProducer->m_ctx = c;
     m_level = -1;
+    check(wap_set_tuning(c, "flow_bits", m_flow_bits), c, "flow precision");
   }
 
   // The whole reconstruction (WaP_Tomo.cpp:473-875); the reference ends the
@@ -509,6 +510,7 @@ class PSART {
   int m_flow_scales = 5;
   int m_flow_iters = 3000;
   float m_flow_tol = 0.008f;
+  int m_flow_bits = 32;   // 16: the precision form (FP16 flow-solver state); set before SetData
   bool m_dump = true;     // write the reference's Analyze dumps (SART, flow, warped, WaP)
   std::string m_out;
   wap_stats m_stats{};

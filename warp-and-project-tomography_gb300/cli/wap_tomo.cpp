@@ -60,6 +60,7 @@ const Opt kOpts[] = {
     {0, "flow-iters", 1, 1, "[ext] primal-dual iterations per flow level (default 3000)"},
     {0, "flow-scales", 1, 1, "[ext] flow pyramid levels (default 5)"},
     {0, "save-final", 3, 1, "[ext] write PREFIX.level%02d.f%03d.{vol,flow}.hdr after the last level"},
+    {0, "flow-bits", 1, 1, "[ext] {32,16}: 16 = the precision form (FP16 flow-solver state; default 32)"},
 };
 
 struct Values {
@@ -243,6 +244,11 @@ int main(int argc, char **argv) {
     scene.m_bp_exact = arith == "exact" ? 1 : 0;
     scene.m_flow_iters = integer(vals, "flow-iters", 0, 3000);
     scene.m_flow_scales = integer(vals, "flow-scales", 0, 5);
+    scene.m_flow_bits = integer(vals, "flow-bits", 0, 32);
+    if (scene.m_flow_bits != 32 && scene.m_flow_bits != 16) {
+      std::printf("wap_tomo: --flow-bits must be 32 or 16\n");
+      return 1;
+    }
     // Render's local nb_proxiSART is 2 whatever -p says (WaP_Tomo.cpp:484)
     scene.SetData(&data);
     scene.Render();
