@@ -114,6 +114,14 @@ WAP_API int wap_set_profiling(wap_ctx *ctx, int on);
  * the scan-dependent calls return WAP_ESTATE on it. */
 WAP_API int wap_create_compute(wap_ctx **out, int device);
 
+/* Device memory of destroyed contexts is kept in a process-wide cache and
+ * reused by later contexts (cudaFree would synchronise the whole device).
+ * wap_cached_bytes: bytes held there; wap_trim_cache(device): frees them
+ * (device < 0: all devices) and returns the bytes freed.  A failed
+ * allocation empties the cache of its device and retries by itself. */
+WAP_API size_t wap_cached_bytes(void);
+WAP_API size_t wap_trim_cache(int device);
+
 /* Device memory helpers, so that callers need no CUDA headers: allocation on
  * the context's device, and copies ordered on the context's stream that
  * return when the copy is complete. */

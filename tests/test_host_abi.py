@@ -116,3 +116,9 @@ def test_server_without_a_gpu_is_an_error(wapmod, torch_available=None):
         pytest.skip("a GPU is present")
     with pytest.raises(wapmod.WapError):
         wapmod.Server(1 << 30, workers=1)
+
+
+def test_block_cache_is_empty_without_contexts(wapmod):
+    L = wapmod.load()
+    assert L.wap_trim_cache(-1) == 0
+    assert L.wap_cached_bytes() == 0

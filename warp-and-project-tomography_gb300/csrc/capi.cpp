@@ -31,14 +31,74 @@ using namespace wap;
 
 namespace {
 
+// Device blocks of destroyed contexts, kept for the next context instead of
+// cudaFree, which synchronises the whole device (and so would stall every
+// other reconstruction of a request loop each time one finishes).  Only
+// wap_destroy recycles, after the context's stream has drained; keyed by
+// (device, capacity); a request takes the smallest block that fits with at
+// most 1/8 (or 2 MiB) slack.  An allocation that fails empties the cache of
+// that device and retries.
+std::mutex g_cache_mu;
+std::multimap<std::pair<int, size_t>, void *> g_cache;
+size_t g_cache_bytes = 0;
+thread_local bool g_recycle = false;
+
+void *cache_take(size_t b, size_t &cap) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  auto it = g_cache.lower_bound(std::make_pair(dev, b));
+  if (it == g_cache.end() || it->first.first != dev || it->first.second > b + std::max(b / 8, (size_t)2 << 20))
+    return nullptr;
+  cap = it->first.second;
+  void *p = it->second;
+  g_cache.erase(it);
+  g_cache_bytes -= cap;
+  return p;
+}
+
+void cache_put(void *p, size_t cap) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaFree(p);
+    return;
+  }
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  g_cache.emplace(std::make_pair(dev, cap), p);
+  g_cache_bytes += cap;
+}
+
+size_t cache_trim(int dev) {  // dev < 0: every device
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  size_t freed = 0;
+  for (auto it = g_cache.begin(); it != g_cache.end();) {
+    if (dev >= 0 && it->first.first != dev) {
+      ++it;
+      continue;
+    }
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(it->first.first);
+    cudaFree(it->second);
+    cudaSetDevice(cur);
+    freed += it->first.second;
+    g_cache_bytes -= it->first.second;
+    it = g_cache.erase(it);
+  }
+  return freed;
+}
+
 struct DevMem {
   void *p = nullptr;
   size_t bytes = 0;
   DevMem() = default;
   DevMem(const DevMem &) = delete;
   DevMem &operator=(const DevMem &) = delete;
-  ~DevMem() { release(); }
-  void release() {
+  ~DevMem() {
+    if (p && g_recycle) cache_put(p, bytes);
+    else release();
+  }
+  void release() {  // in-flight work may still use the block: a synchronising free
     if (p) cudaFree(p);
     p = nullptr;
     bytes = 0;
@@ -46,8 +106,20 @@ struct DevMem {
   cudaError_t ensure(size_t b) {
     if (b <= bytes && p) return cudaSuccess;
     release();
-    cudaError_t e = cudaMalloc(&p, b ? b : 16);
-    if (e == cudaSuccess) bytes = b;
+    const size_t want = b ? b : 16;
+    size_t cap = 0;
+    if ((p = cache_take(want, cap)) != nullptr) {
+      bytes = cap;
+      return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaErrorMemoryAllocation) {
+      cudaGetLastError();
+      int dev = 0;
+      cudaGetDevice(&dev);
+      if (cache_trim(dev) > 0) e = cudaMalloc(&p, want);
+    }
+    if (e == cudaSuccess) bytes = want;
     else p = nullptr;
     return e;
   }
@@ -119,6 +191,8 @@ struct wap_ctx {
   std::map<std::tuple<int, int, int>, std::unique_ptr<FlowWork>> flow_work;
   std::vector<std::unique_ptr<PyramidLevel>> pyramid;
   DevMem blur_a, blur_b, rs_a, rs_b;
+  DevMem pyr_b1, pyr_b2;  // blurred full-size flow inputs
+  DevMem adv_tab;         // cell-centre table of a wap_advect call
   std::map<std::pair<int, int>, std::unique_ptr<DevMem[]>> resize_tables;
   DevMem cg_buf;
 
@@ -754,7 +828,7 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
   }
   // blur at full resolution, then build the pyramid (optical_flow.h:1010-1052)
   PyramidLevel &fine = *ctx->pyramid[scales - 1];
-  DevMem b1, b2;
+  DevMem &b1 = ctx->pyr_b1, &b2 = ctx->pyr_b2;  // persistent: no allocation (and no free) per pair
   CU(b1.ensure(sizeof(float) * nv));
   CU(b2.ensure(sizeof(float) * nv));
   TRY(do_blur(ctx, dims, 1, sigma, I1, b1.as<float>()));
@@ -804,7 +878,7 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
     }
   }
   CU(cudaMemcpyAsync(Vout, fine.v.p, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));  // b1/b2 are released on return
+  CU(cudaStreamSynchronize(ctx->stream));
   for (int l = 0; l < scales; ++l) {
     float ms = 0.0f;
     CU(cudaEventElapsedTime(&ms, lev[l], lev[l + 1]));
@@ -1007,12 +1081,21 @@ int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user) {
 void wap_destroy(wap_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
-  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  const bool idle = !ctx->stream || cudaStreamSynchronize(ctx->stream) == cudaSuccess;
   cudaStream_t s = ctx->own_stream ? ctx->stream : nullptr;
   for (cudaEvent_t e : ctx->pd_events) cudaEventDestroy(e);
+  g_recycle = idle;  // the stream has drained: the blocks go to the cache
   delete ctx;
+  g_recycle = false;
   if (s) cudaStreamDestroy(s);
 }
+
+size_t wap_cached_bytes(void) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  return g_cache_bytes;
+}
+
+size_t wap_trim_cache(int device) { return cache_trim(device); }
 
 const char *wap_last_error(const wap_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
@@ -1309,12 +1392,11 @@ int wap_advect(wap_ctx *ctx, const int *dims, const float *aabb, const float *d_
   CHECK(aabb[1] > aabb[0] && aabb[3] > aabb[2] && aabb[5] > aabb[4], WAP_EINVAL, "empty bounding box");
   std::vector<float> h(dims[0] + dims[1] + dims[2]);
   world_table(dims, aabb, h.data());
-  DevMem tab;
-  TRY(upload(ctx, tab, h));
+  TRY(upload(ctx, ctx->adv_tab, h));
   std::vector<AdvectJob> jobs{AdvectJob{d_vel, d_src, d_out, dt}};
   TRY(upload(ctx, ctx->jobs_misc, jobs));
-  KL(launch_advect(dims, aabb, tab.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, nc, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));  // the table is released on return
+  KL(launch_advect(dims, aabb, ctx->adv_tab.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, nc, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));  // the host table and job list are reused by the next call
   return WAP_OK;
 }
 
@@ -1457,7 +1539,8 @@ size_t wap_ctx_device_bytes(const wap_ctx *ctx) {
   for (const DevMem *m : {&ctx->geom, &ctx->projs_own, &ctx->vols, &ctx->flows, &ctx->ytv, &ctx->ytp, &ctx->xbar,
                           &ctx->xprev, &ctx->zero_vol, &ctx->dual, &ctx->corr, &ctx->warped, &ctx->delta, &ctx->back,
                           &ctx->jobs_fp, &ctx->jobs_bp, &ctx->jobs_adv, &ctx->jobs_acc, &ctx->jobs_misc, &ctx->world,
-                          &ctx->maxbits, &ctx->blur_a, &ctx->blur_b, &ctx->rs_a, &ctx->rs_b, &ctx->cg_buf})
+                          &ctx->maxbits, &ctx->blur_a, &ctx->blur_b, &ctx->rs_a, &ctx->rs_b, &ctx->cg_buf,
+                          &ctx->pyr_b1, &ctx->pyr_b2, &ctx->adv_tab})
     b += m->bytes;
   for (const auto &kv : ctx->flow_work) {
     const FlowWork &w = *kv.second;

@@ -203,6 +203,7 @@ void wap_server_destroy(wap_server *s) {
   s->cv.notify_all();
   for (auto &t : s->workers) t.join();
   for (auto &kv : s->jobs) s->release_ctx(kv.second.get());
+  wap_trim_cache(s->device);  // the jobs' recycled device blocks
   delete s;
 }
 

@@ -95,6 +95,8 @@ WAP_EV_SART, WAP_EV_FLOW, WAP_EV_WARP = 1, 2, 3
 # Every function declared in include/wap/wap.h, with its ctypes signature.
 SIGNATURES = {
     "wap_create_compute": (_c_int, [ctypes.POINTER(_vp), _c_int]),
+    "wap_cached_bytes": (ctypes.c_size_t, []),
+    "wap_trim_cache": (ctypes.c_size_t, [_c_int]),
     "wap_alloc": (_c_int, [_vp, ctypes.c_size_t, ctypes.POINTER(_vp)]),
     "wap_free": (_c_int, [_vp, _vp]),
     "wap_copy_to_device": (_c_int, [_vp, _vp, _vp, ctypes.c_size_t]),
