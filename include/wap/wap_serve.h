@@ -46,7 +46,8 @@ typedef struct {
  * level, scratch): the admission footprint. */
 WAP_API size_t wap_job_device_bytes(const wap_scan_desc *scan, const wap_schedule *sched);
 
-/* Device bytes a context holds now. */
+/* Device bytes a context has asked for and holds now (a block reused from the
+ * process's cache of freed blocks may be up to 1/8 larger than asked). */
 WAP_API size_t wap_ctx_device_bytes(const wap_ctx *ctx);
 
 /* workers: host threads stepping jobs (each job is stepped by one thread at

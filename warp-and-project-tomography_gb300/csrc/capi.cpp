@@ -48,8 +48,10 @@ void *cache_take(size_t b, size_t &cap) {
   if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
   std::lock_guard<std::mutex> lk(g_cache_mu);
   auto it = g_cache.lower_bound(std::make_pair(dev, b));
-  if (it == g_cache.end() || it->first.first != dev || it->first.second > b + std::max(b / 8, (size_t)2 << 20))
-    return nullptr;
+  // blocks of 1 MiB or more may come from a cached block up to 1/8 larger;
+  // smaller requests take only a block of their own size
+  const size_t slack = b >= ((size_t)1 << 20) ? b / 8 : 0;
+  if (it == g_cache.end() || it->first.first != dev || it->first.second > b + slack) return nullptr;
   cap = it->first.second;
   void *p = it->second;
   g_cache.erase(it);
@@ -90,7 +92,8 @@ size_t cache_trim(int dev) {  // dev < 0: every device
 
 struct DevMem {
   void *p = nullptr;
-  size_t bytes = 0;
+  size_t bytes = 0;  // capacity
+  size_t want = 0;   // the largest size asked of this block since it was (re)allocated
   DevMem() = default;
   DevMem(const DevMem &) = delete;
   DevMem &operator=(const DevMem &) = delete;
@@ -101,25 +104,29 @@ struct DevMem {
   void release() {  // in-flight work may still use the block: a synchronising free
     if (p) cudaFree(p);
     p = nullptr;
-    bytes = 0;
+    bytes = want = 0;
   }
   cudaError_t ensure(size_t b) {
-    if (b <= bytes && p) return cudaSuccess;
-    release();
-    const size_t want = b ? b : 16;
-    size_t cap = 0;
-    if ((p = cache_take(want, cap)) != nullptr) {
-      bytes = cap;
+    if (b <= bytes && p) {
+      want = std::max(want, b);
       return cudaSuccess;
     }
-    cudaError_t e = cudaMalloc(&p, want);
+    release();
+    const size_t ask = b ? b : 16;
+    size_t cap = 0;
+    if ((p = cache_take(ask, cap)) != nullptr) {
+      bytes = cap;
+      want = ask;
+      return cudaSuccess;
+    }
+    cudaError_t e = cudaMalloc(&p, ask);
     if (e == cudaErrorMemoryAllocation) {
       cudaGetLastError();
       int dev = 0;
       cudaGetDevice(&dev);
-      if (cache_trim(dev) > 0) e = cudaMalloc(&p, want);
+      if (cache_trim(dev) > 0) e = cudaMalloc(&p, ask);
     }
-    if (e == cudaSuccess) bytes = want;
+    if (e == cudaSuccess) bytes = want = ask;
     else p = nullptr;
     return e;
   }
@@ -563,9 +570,13 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
     return WAP_OK;
   }
   std::vector<std::pair<int, int>> cand;
+  // TMA-form chunks: the kernel time is flat within a few per cent from about
+  // a quarter to half of zt (short chunks repeat a plane's primal, long ones
+  // leave a partial last wave), so the candidates span zt/4..zt.
+  const int zts[4] = {zt / 4, zt / 3, zt / 2, zt};
   if (half) {
-    for (int z : {zt / 2, zt, zt * 2})
-      if (z >= 2 && z <= n[2]) cand.emplace_back(4, z);
+    for (int z : zts)
+      if (z >= 2 && z <= n[2] && (cand.empty() || cand.back().second != z)) cand.emplace_back(4, z);
     if (cand.empty()) cand.emplace_back(4, std::max(1, n[2]));
   } else {
     for (int z : {zf / 2, zf, zf * 2})
@@ -573,8 +584,8 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
     for (int z : {zs / 2, zs, zs * 2, zs * 4})
       if (z >= 1 && z <= n[2]) cand.emplace_back(2, z);
     if (tma)
-      for (int z : {zt / 2, zt, zt * 2})
-        if (z >= 2 && z <= n[2]) cand.emplace_back(3, z);
+      for (int z : zts)
+        if (z >= 2 && z <= n[2] && (cand.back().first != 3 || cand.back().second != z)) cand.emplace_back(3, z);
   }
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
@@ -1541,17 +1552,17 @@ size_t wap_ctx_device_bytes(const wap_ctx *ctx) {
                           &ctx->jobs_fp, &ctx->jobs_bp, &ctx->jobs_adv, &ctx->jobs_acc, &ctx->jobs_misc, &ctx->world,
                           &ctx->maxbits, &ctx->blur_a, &ctx->blur_b, &ctx->rs_a, &ctx->rs_b, &ctx->cg_buf,
                           &ctx->pyr_b1, &ctx->pyr_b2, &ctx->adv_tab})
-    b += m->bytes;
+    b += m->want;
   for (const auto &kv : ctx->flow_work) {
     const FlowWork &w = *kv.second;
     for (const DevMem *m : {&w.va, &w.vb, &w.y, &w.y2, &w.u, &w.kty, &w.kx4prev, &w.warp, &w.acc, &w.err, &w.world})
-      b += m->bytes;
+      b += m->want;
   }
   for (const auto &p : ctx->pyramid)
     if (p)
-      for (const DevMem *m : {&p->i1, &p->i2, &p->v, &p->y}) b += m->bytes;
+      for (const DevMem *m : {&p->i1, &p->i2, &p->v, &p->y}) b += m->want;
   for (const auto &kv : ctx->resize_tables)
-    for (int q = 0; q < 5; ++q) b += kv.second[q].bytes;
+    for (int q = 0; q < 5; ++q) b += kv.second[q].want;
   return b;
 }
 
