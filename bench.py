@@ -54,7 +54,7 @@ PD_BYTES_MIN_PER_VOXEL = 4 * (10 + 10 + 3 + 3 + 4)
 # DRAM bytes (read + write) of one primal-dual iteration at 256^3 per kernel
 # form (1 fused, 2 primal + dual, 3 TMA-fed fused), from ncu captures (dram__bytes_read.sum +
 # dram__bytes_write.sum) of kernel_bench.py.
-PD_TRAFFIC_256 = {1: 1.98e9, 2: 3.29e9, 3: 1.98e9}
+PD_TRAFFIC_256 = {1: 1.98e9, 2: 3.29e9, 3: 1.95e9}
 PD_FORMS = {1: "pd_fused_kernel", 2: "pd_primal_kernel + pd_dual_kernel", 3: "pd_tma_kernel (TMA-fed fused)"}
 
 
@@ -333,17 +333,22 @@ def run_gb300(args):
         tdist.barrier()
     K = args.steps
     value = replicas.aggregate_rate(world, K / F, t_dev)
+    pd_side = round(pd_vox ** (1.0 / 3.0))
+    form, zchunk = ctx.get_tuning([pd_side] * 3)
     precision = None
     if world == 1 and args.precision_steps > 0 and args.flow_bits == 32:
-        # The same frame-steps again with the flow solver's state in FP16.
+        # The same frame-steps again in the precision form: the flow solver's
+        # state in FP16 with its fast arithmetic, and the FP32 backprojection.
         ctx.set_tuning("flow_bits", 16)
+        sched16 = wap.reference_schedule(n_cp=5, nb_sart=2, wp_frames=F, flow_iters=args.flow_iters,
+                                         flow_scales=args.scales, flow_tol=0.008, cut=8, bp_exact=0)
         t16 = 0.0
         for i in range(args.warmup, args.warmup + args.precision_steps):
             f = order[args.warmup + (i - args.warmup) % args.steps]
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(stream):
                 e0.record(stream)
-            ctx.outer_iteration_frames(sched, f, f + 1)
+            ctx.outer_iteration_frames(sched16, f, f + 1)
             with torch.cuda.stream(stream):
                 e1.record(stream)
             stream.synchronize()
@@ -353,13 +358,13 @@ def run_gb300(args):
         precision = {"flow_bits": 16, "value": v16, "unit": "outer-iter/s", "ms_per_step": t16 / args.precision_steps * 1e3,
                      "speedup_vs_fp32": v16 / value,
                      "note": "the timed frames re-run with the flow solver's dual, flow and linearisation stored in "
-                             "FP16 (FP32 arithmetic); accuracy: tests/test_gpu_parity.py::test_precision_form_*"}
+                             "FP16 (FP32 fused multiply-adds and hardware reciprocals in the primal-dual iteration) "
+                             "and the FP32 backprojection in place of the reference's double bicubic; accuracy: "
+                             "tests/test_gpu_parity.py::test_precision_form_*"}
     e2e = replicas.aggregate_rate(world, K / F, t_e2e)
     pd_ms = agg["ms_pd"] / max(agg["pd_timed"], 1)
     achieved = PD_BYTES_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
-    pd_side = round(pd_vox ** (1.0 / 3.0))
-    form, zchunk = ctx.get_tuning([pd_side] * 3)
     result = {
         "metric": METRIC, "value": value, "unit": "outer-iter/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": t_dev / K * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -381,6 +386,10 @@ def run_gb300(args):
                      "algorithmic_bytes": PD_BYTES_PER_VOXEL * pd_vox, "bytes_per_voxel": PD_BYTES_PER_VOXEL,
                      "min_bytes_per_voxel": PD_BYTES_MIN_PER_VOXEL,
                      "frac_at_min_bytes": PD_BYTES_MIN_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9 / peak,
+                     "note": "achieved counts the 208 B/voxel two-kernel contract bytes; the fused single-pass "
+                             "kernel reads and writes each word once (120 B/voxel, traffic = measured DRAM bytes "
+                             "of one launch), so frac above 1 is the fusion's saving and frac_at_min_bytes is the "
+                             "fraction of the measured copy bandwidth on the bytes it moves",
                      "ms_per_launch": pd_ms, "launches_timed": int(agg["pd_timed"])},
         "phase_ms_per_step": {"cp_sart": agg["ms_cp"] / K, "flow": agg["ms_flow"] / K, "wap": agg["ms_wap"] / K},
         "pd_iterations_per_step": agg["flow_pd_iterations"] / K,

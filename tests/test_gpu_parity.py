@@ -348,10 +348,11 @@ def test_cg_screened_laplacian(setup, orc, mode):
 
 
 def test_precision_form_fp16_flow_state(setup, orc, wapmod):
-    """The precision form (flow solver state in FP16, FP32 arithmetic): same
-    iteration counts at a fixed count, the flow within the stated tolerance of
-    the FP32 path, and an outer iteration's volumes within 1e-3 relative L2 of
-    the oracle."""
+    """The precision form (flow solver state in FP16; FP32 arithmetic with
+    fused multiply-adds and hardware reciprocals in the primal-dual iteration):
+    same iteration counts at a fixed count, the flow within 2e-2 relative L2
+    of the exact FP32 path, and an outer iteration's volumes within 1e-3
+    relative L2 of the oracle."""
     s = setup
     torch, ctx = s["torch"], s["ctx"]
     aabb, I1, I2 = _flow_inputs(s, orc)

@@ -1149,9 +1149,10 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
   if (k == "pd_form") {
     CHECK(value >= 0 && value <= 3, WAP_EINVAL, "pd_form must be 0, 1, 2 or 3");
     ctx->pd_form = value;
-  } else if (k == "flow_bits") {
+  } else if (k == "flow_bits") {  // each precision keeps its own tuned plans
     CHECK(value == 32 || value == 16, WAP_EINVAL, "flow_bits must be 32 or 16");
     ctx->flow_bits = value;
+    return WAP_OK;
   } else if (k == "pd_zchunk") {
     CHECK(value >= 0, WAP_EINVAL, "pd_zchunk must be >= 0");
     ctx->pd_zchunk = value;
