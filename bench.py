@@ -335,6 +335,7 @@ def run_gb300(args):
     value = replicas.aggregate_rate(world, K / F, t_dev)
     pd_side = round(pd_vox ** (1.0 / 3.0))
     form, zchunk = ctx.get_tuning([pd_side] * 3)
+    level_plans = [list(ctx.get_tuning([int(n * 0.5 ** l)] * 3)) for l in range(args.scales)]
     precision = None
     if world == 1 and args.precision_steps > 0 and args.flow_bits == 32:
         # The same frame-steps again in the precision form: the flow solver's
@@ -395,7 +396,8 @@ def run_gb300(args):
         "pd_iterations_per_step": agg["flow_pd_iterations"] / K,
         "flow_levels_finest_first": {"sides": [int(n * 0.5 ** l) for l in range(args.scales)],
                                      "ms_per_step": [v / K for v in lev_ms],
-                                     "pd_iterations_per_step": [v / K for v in lev_its]},
+                                     "pd_iterations_per_step": [v / K for v in lev_its],
+                                     "pd_form_and_zchunk": level_plans},
         "op_counts_per_outer_iteration": {k: agg[k] * F / K for k in ("projections", "backprojections",
                                                                        "advect_voxels", "cp_frame_passes",
                                                                        "pd_voxel_iters")},

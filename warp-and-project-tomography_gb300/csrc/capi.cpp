@@ -572,8 +572,23 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
   std::vector<std::pair<int, int>> cand;
   // TMA-form chunks: the kernel time is flat within a few per cent from about
   // a quarter to half of zt (short chunks repeat a plane's primal, long ones
-  // leave a partial last wave), so the candidates span zt/4..zt.
-  const int zts[4] = {zt / 4, zt / 3, zt / 2, zt};
+  // leave a partial last wave), so the candidates span zt/4..zt, plus the two
+  // chunk lengths (4..64 planes) whose chunk counts come closest to filling
+  // whole waves of resident blocks (the kernel balances the chunk lengths).
+  std::vector<int> zts = {zt / 4, zt / 3, zt / 2, zt};
+  if (tma || half) {
+    const int slots = pd_tma_slots(half), tiles = pd_tma_tiles(D);
+    std::vector<std::pair<double, int>> waves;  // (-wave fill, rounded; z-chunk)
+    for (int nc = 1; slots > 0 && nc <= n[2] / 4; ++nc) {
+      const int z = (n[2] + nc - 1) / nc;
+      if ((n[2] + z - 1) / z != nc || z > 64) continue;  // not a grid of nc chunks
+      const double w = (double)tiles * nc / slots, fill = w / std::ceil(w);
+      if (fill >= 0.96) waves.emplace_back(-std::round(fill * 100.0) - std::fabs(z - zt / 2.0) * 1e-3, z);
+    }
+    std::sort(waves.begin(), waves.end());
+    for (size_t q = 0; q < waves.size() && q < 2; ++q)
+      if (std::find(zts.begin(), zts.end(), waves[q].second) == zts.end()) zts.push_back(waves[q].second);
+  }
   if (half) {
     for (int z : zts)
       if (z >= 2 && z <= n[2] && (cand.empty() || cand.back().second != z)) cand.emplace_back(4, z);

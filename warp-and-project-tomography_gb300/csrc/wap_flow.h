@@ -50,9 +50,14 @@ cudaError_t launch_pd_split(const FlowDims &D, int zchunk, const float *yin, flo
 struct alignas(64) PdTmaMap {
   unsigned char bytes[128];
 };
-// half = the precision form: y, u, v stored in FP16 (nx % 8 == 0), FP32
-// arithmetic; otherwise FP32 storage (nx % 4 == 0).
+// half = the precision form: y, u, v stored in FP16 (nx % 8 == 0) with the
+// fast FP32 arithmetic; otherwise FP32 storage (nx % 4 == 0), exact.
 bool pd_tma_supported(const FlowDims &D, bool half);
+// Blocks of the TMA form resident on the whole GPU at once (SMs x blocks per
+// SM; 0 if the query fails) and the (x, y) tiles of a grid: a z-chunk count
+// making tiles x chunks a multiple of the slots fills whole waves.
+int pd_tma_slots(bool half);
+int pd_tma_tiles(const FlowDims &D);
 cudaError_t make_pd_tma_maps(const FlowDims &D, bool half, const void *y, const void *u, const void *v, void *ymap,
                              void *umap, void *vmap);
 cudaError_t launch_pd_tma(const FlowDims &D, int zchunk, bool half, const void *ymap, const void *umap,
