@@ -16,11 +16,10 @@ static float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
 static uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 static float shrink_fast(float a, float den, float rinv, int *bad) {
   const float q0 = a * rinv;
-  const float e = fmaf(-q0, den, a);
-  const float q = fmaf(e, rinv, q0);
-  const int zero = a == 0.0f;
-  *bad |= !(zero || (fabsf(a) >= 1.0e-30f && fabsf(q0) < 3.0e38f));
-  return zero ? q0 : q;
+  const float en = fmaf(q0, den, -a);
+  const float q = fmaf(-en, rinv, q0);
+  *bad |= (a != 0.0f && fabsf(a) < 1.0e-30f) || !(fabsf(q0) < 3.0e38f);
+  return q;
 }
 static float shrink_tiny(float a, float den, float rinv) {
   const float a2 = a * 0x1p64f;

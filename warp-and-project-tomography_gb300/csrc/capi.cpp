@@ -143,6 +143,11 @@ struct Status {
 // Exhaustive proofs of the fast division paths, per (device, key).
 std::mutex g_proof_mutex;
 std::map<std::pair<int, uint64_t>, int> g_proofs;
+// Autotuned primal-dual plans shared by every context of the process, so a
+// request loop's jobs tune each grid size once: (device, nx, ny, nz, FP16
+// storage, TMA form available) -> (form, z-chunk).
+std::mutex g_plan_mutex;
+std::map<std::tuple<int, int, int, int, int, int>, std::pair<int, int>> g_plans;
 
 // Flow-solver workspace for one grid size (reused across pairs and calls).
 struct FlowWork {
@@ -569,6 +574,17 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
     zchunk = it->second.second;
     return WAP_OK;
   }
+  const auto gkey = std::make_tuple(ctx->device, n[0], n[1], n[2], half ? 1 : 0, tma ? 1 : 0);
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mutex);
+    auto g = g_plans.find(gkey);
+    if (g != g_plans.end()) {
+      plans[key] = g->second;
+      form = g->second.first;
+      zchunk = g->second.second;
+      return WAP_OK;
+    }
+  }
   std::vector<std::pair<int, int>> cand;
   // TMA-form chunks: the kernel time is flat within a few per cent from about
   // a quarter to half of zt (short chunks repeat a plane's primal, long ones
@@ -623,6 +639,10 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   plans[key] = pick;
+  {
+    std::lock_guard<std::mutex> lk(g_plan_mutex);
+    g_plans[gkey] = pick;
+  }
   form = pick.first;
   zchunk = pick.second;
   return WAP_OK;
