@@ -55,7 +55,8 @@ PD_BYTES_MIN_PER_VOXEL = 4 * (10 + 10 + 3 + 3 + 4)
 # form (1 fused, 2 primal + dual, 3 TMA-fed fused), from ncu captures (dram__bytes_read.sum +
 # dram__bytes_write.sum) of kernel_bench.py.
 PD_TRAFFIC_256 = {1: 1.98e9, 2: 3.29e9, 3: 1.95e9}
-PD_FORMS = {1: "pd_fused_kernel", 2: "pd_primal_kernel + pd_dual_kernel", 3: "pd_tma_kernel (TMA-fed fused)"}
+PD_FORMS = {1: "pd_fused_kernel", 2: "pd_primal_kernel + pd_dual_kernel", 3: "pd_tma_kernel (TMA-fed fused)",
+            4: "pd_tma_kernel<__half> (precision form)"}
 
 
 def parse():

@@ -104,8 +104,10 @@ WAP_API const char *wap_last_error(const wap_ctx *ctx);
 WAP_API int wap_set_stream(wap_ctx *ctx, void *cuda_stream);
 WAP_API int wap_synchronize(wap_ctx *ctx);
 WAP_API int wap_get_stats(wap_ctx *ctx, wap_stats *out);
-/* 1: time every primal-dual iteration of the flow solver with CUDA events on
- * the context's stream (wap_stats.ms_pd); 0 (default): no per-launch events. */
+/* 1: time primal-dual iterations of the flow solver at the largest grid with
+ * CUDA events on the context's stream (every tenth launch, so the others
+ * keep their programmatic overlap; wap_stats.ms_pd / pd_timed is the mean
+ * launch time); 0 (default): no per-launch events. */
 WAP_API int wap_set_profiling(wap_ctx *ctx, int on);
 
 /* A context without a scan, for the calls that take their grid as arguments

@@ -811,10 +811,14 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
       const int res = (it % 50 == 0);
       const int store = ((it + 1) % 50 == 0);
       if (res) CU(cudaMemsetAsync(acc, 0, sizeof(double) * 2, ctx->stream));
-      if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending], ctx->stream));
+      // Timed launches: every tenth, so that the events between launches
+      // leave the others free to overlap their start with the previous
+      // grid's tail (programmatic dependent launch).
+      const bool timed = prof && pending < 50 && it % 10 == 3;
+      if (timed) CU(cudaEventRecord(ctx->pd_events[2 * pending], ctx->stream));
       const int mode = (it == 1) ? (wi == 0 ? 1 : 2) : 0;
       KL(pd_launch(form, zchunk, mode, store, res));
-      if (prof && pending < 50) CU(cudaEventRecord(ctx->pd_events[2 * pending++ + 1], ctx->stream));
+      if (timed) CU(cudaEventRecord(ctx->pd_events[2 * pending++ + 1], ctx->stream));
       std::swap(vcur, vnext);
       std::swap(ycur, ynext);
       if (res) {
@@ -1201,9 +1205,10 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
 
 int wap_get_tuning(wap_ctx *ctx, const int *dims, int *h_form, int *h_zchunk) {
   CHECK(ctx && dims && h_form && h_zchunk, WAP_EINVAL, "null argument");
-  auto it = ctx->pd_plans.find(std::make_tuple(dims[0], dims[1], dims[2]));
-  *h_form = it == ctx->pd_plans.end() ? ctx->pd_form : it->second.first;
-  *h_zchunk = it == ctx->pd_plans.end() ? ctx->pd_zchunk : it->second.second;
+  const auto &plans = ctx->flow_bits == 16 ? ctx->pd_plans16 : ctx->pd_plans;  // the current precision's plans
+  auto it = plans.find(std::make_tuple(dims[0], dims[1], dims[2]));
+  *h_form = it == plans.end() ? ctx->pd_form : it->second.first;
+  *h_zchunk = it == plans.end() ? ctx->pd_zchunk : it->second.second;
   return WAP_OK;
 }
 
