@@ -161,9 +161,9 @@ WAP_API int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user);
  * TMA-fed fused kernel (grids with nx % 4 == 0, else 2); "pd_zchunk": z
  * planes per block, 0 = autotuned / default.  One key changes results: the
  * precision form, "flow_bits" = 16 stores the flow solver's dual, flow and
- * linearisation in FP16 during the primal-dual iterations and computes them
- * with fused multiply-adds and hardware reciprocals (FP64 residual sums;
- * grids with nx % 8 == 0, others stay FP32); 32 (the default) is the
+ * linearisation as FP16 pairs during the primal-dual iterations and computes
+ * them with fused multiply-adds and hardware reciprocals (FP64 residual sums;
+ * grids with nx % 4 == 0, others stay FP32); 32 (the default) is the
  * reference's arithmetic.  Each precision keeps its own autotuned plans.
  * Unknown keys are WAP_EINVAL. */
 WAP_API int wap_set_tuning(wap_ctx *ctx, const char *key, int value);

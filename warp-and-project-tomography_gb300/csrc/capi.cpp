@@ -732,8 +732,8 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   if (ctx->flow_bits == 16 && w->h_state == 0) {
     w->h_state = -1;
     if (pd_tma_supported(D, true) && w->tma_err.ensure(sizeof(int)) == cudaSuccess &&
-        w->yh[0].ensure(2 * 10 * nv) == cudaSuccess && w->yh[1].ensure(2 * 10 * nv) == cudaSuccess &&
-        w->vh[0].ensure(2 * 3 * nv) == cudaSuccess && w->vh[1].ensure(2 * 3 * nv) == cudaSuccess &&
+        w->yh[0].ensure(4 * 5 * nv) == cudaSuccess && w->yh[1].ensure(4 * 5 * nv) == cudaSuccess &&
+        w->vh[0].ensure(4 * 2 * nv) == cudaSuccess && w->vh[1].ensure(4 * 2 * nv) == cudaSuccess &&
         w->uh.ensure(2 * 4 * nv) == cudaSuccess &&
         make_pd_tma_maps(D, true, w->yh[0].p, w->uh.p, w->vh[0].p, &w->hymap[0], &w->humap, &w->hvmap[0]) ==
             cudaSuccess &&
@@ -745,9 +745,9 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   }
   const bool half = ctx->flow_bits == 16 && w->h_state == 1;
   if (half) {
-    KL(launch_to_half(10 * nv, y, w->yh[0].p, ctx->stream));
-    KL(launch_to_half(3 * nv, w->va.as<float>(), w->vh[0].p, ctx->stream));
-    KL(launch_to_half(3 * nv, w->vb.as<float>(), w->vh[1].p, ctx->stream));
+    KL(launch_to_pairs(nv, 10, y, w->yh[0].p, ctx->stream));
+    KL(launch_to_pairs(nv, 3, w->va.as<float>(), w->vh[0].p, ctx->stream));
+    KL(launch_to_pairs(nv, 3, w->vb.as<float>(), w->vh[1].p, ctx->stream));
   }
   auto pd_launch = [&](int f, int zc, int mode, int store, int res) -> cudaError_t {
     const int yi = ycur == w->y.as<float>() ? 0 : 1, vi = vcur == w->va.as<float>() ? 0 : 1;
@@ -776,7 +776,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream));
     ctx->stats.advect_voxels += (double)nv;
     KL(launch_linearize(D, w->warp.as<float>(), I1, vcur, w->u.as<float>(), w->kx4prev.as<float>(), ctx->stream));
-    if (half) KL(launch_to_half(4 * nv, w->u.as<float>(), w->uh.p, ctx->stream));
+    if (half) KL(launch_to_pairs(nv, 4, w->u.as<float>(), w->uh.p, ctx->stream));
     if (wi == 0 && max_iters >= 0) {
       TRY(pd_plan(ctx, D, pd_launch, form, zchunk, w->tma_state == 1, half));
       if (w->tma_state == 1 || half) {  // a tuning launch of the TMA form must not have timed out either
@@ -832,7 +832,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
       CU(cudaStreamSynchronize(ctx->stream));
       TRY(drain());
     }
-    if (half) KL(launch_from_half(3 * nv, w->vh[vcur == w->va.as<float>() ? 0 : 1].p, vcur, ctx->stream));
+    if (half) KL(launch_from_pairs(nv, 3, w->vh[vcur == w->va.as<float>() ? 0 : 1].p, vcur, ctx->stream));
     if (form >= 3) {
       int bad = 0;
       CU(cudaMemcpyAsync(&bad, w->tma_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -844,7 +844,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     if (total) *total += it;
     ctx->stats.flow_pd_iterations += it;
   }
-  if (half) KL(launch_from_half(10 * nv, w->yh[ycur == w->y.as<float>() ? 0 : 1].p, ycur, ctx->stream));
+  if (half) KL(launch_from_pairs(nv, 10, w->yh[ycur == w->y.as<float>() ? 0 : 1].p, ycur, ctx->stream));
   CU(cudaMemcpyAsync(V, vcur, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));
   for (int q = 0; q < 3; ++q) KL(launch_roi_copy(D, 3, ycur + 3 * q * nv, Y[q], ctx->stream));
   KL(launch_roi_copy(D, 1, ycur + 9 * nv, Y[3], ctx->stream));

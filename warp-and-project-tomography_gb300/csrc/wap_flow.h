@@ -50,8 +50,8 @@ cudaError_t launch_pd_split(const FlowDims &D, int zchunk, const float *yin, flo
 struct alignas(64) PdTmaMap {
   unsigned char bytes[128];
 };
-// half = the precision form: y, u, v stored in FP16 (nx % 8 == 0) with the
-// fast FP32 arithmetic; otherwise FP32 storage (nx % 4 == 0), exact.
+// half = the precision form: y, u, v stored as FP16 pairs with the fast FP32
+// arithmetic; otherwise FP32 storage, exact.  Both need nx % 4 == 0.
 bool pd_tma_supported(const FlowDims &D, bool half);
 // Blocks of the TMA form resident on the whole GPU at once (SMs x blocks per
 // SM; 0 if the query fails) and the (x, y) tiles of a grid: a z-chunk count
@@ -64,9 +64,11 @@ cudaError_t launch_pd_tma(const FlowDims &D, int zchunk, bool half, const void *
                           const void *vmap, void *yout, void *vout, float *kty, const float *kx4prev, int kxold_mode,
                           float lambda, float sigma1, float rinv, int fastdiv, int rcp, int store_kty, int residual,
                           double *acc, int *err, cudaStream_t st);
-// FP32 <-> FP16 element conversion (round to nearest even).
-cudaError_t launch_to_half(size_t n, const float *src, void *dst, cudaStream_t st);
-cudaError_t launch_from_half(size_t n, const void *src, float *dst, cudaStream_t st);
+// nc component planes of nv floats <-> ceil(nc/2) planes of FP16 pairs
+// (components 2q and 2q+1 in one 32-bit word, an odd last one paired with 0;
+// round to nearest even), the precision form's storage.
+cudaError_t launch_to_pairs(size_t nv, int nc, const float *src, void *dst, cudaStream_t st);
+cudaError_t launch_from_pairs(size_t nv, int nc, const void *src, float *dst, cudaStream_t st);
 // Counts the float inputs for which the FMA-corrected division by den differs
 // from IEEE division (0 proves the fast path exact for this den).
 cudaError_t launch_pd_fastdiv_check(float den, float rinv, unsigned long long *d_bad, cudaStream_t st);
