@@ -422,9 +422,11 @@ def run_gb300(args):
     if rank == 0 and world == 1 and args.serve_jobs > 0:
         # Served form: p50/p95/p99 latency of a Poisson job stream through the
         # request loop (see serving.py for the job mix).
+        # The same stream twice: the reference's arithmetic, then the precision
+        # form (flow_bits 16 per job).
         import serving
-        result["serving"] = serving.run(wap, torch, n_jobs=args.serve_jobs, rate=args.serve_rate,
-                                        workers=args.serve_workers)
+        result["serving"], result["serving_precision"] = serving.run(
+            wap, torch, n_jobs=args.serve_jobs, rate=args.serve_rate, workers=args.serve_workers, flow_bits=(32, 16))
     if rank == 0 and world == 1 and args.batch_jobs > 0:
         # Batched form: uneven scans looped through the plain path vs overlapped
         # through the request loop (same results, checked).

@@ -27,6 +27,8 @@ typedef struct {
   int outer_iterations;   /* outer iterations at time level 0 */
   const double *h_angles; /* scan.nproj angles in degrees, copied at submit */
   const float *h_projs;   /* W*H*nproj projections, copied at submit */
+  int flow_bits;          /* 0 or 32: the reference's arithmetic; 16: the precision form
+                           * (wap_set_tuning "flow_bits") */
 } wap_job_desc;
 
 enum { WAP_JOB_QUEUED = 0, WAP_JOB_RUNNING = 1, WAP_JOB_DONE = 2, WAP_JOB_FAILED = 3 };

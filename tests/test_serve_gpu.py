@@ -21,9 +21,10 @@ def _job(wap, orc, O, n, nproj, seed):
     return scan, sched, ang, projs
 
 
-def _alone(wap, scan, sched, ang, projs, outer):
+def _alone(wap, scan, sched, ang, projs, outer, flow_bits=32):
     ctx = wap.Context(scan, ang)
     try:
+        ctx.set_tuning("flow_bits", flow_bits)
         ctx.upload_projections(projs)
         F = ctx.level_setup(0)
         for _ in range(outer):
@@ -73,5 +74,30 @@ def test_server_rejects_a_job_larger_than_the_budget(wapmod, orc, torch_cuda):
     try:
         with pytest.raises(wap.WapError):
             srv.submit(scan, sched, ang, projs)
+    finally:
+        srv.close()
+
+
+def test_served_precision_form_matches_the_same_jobs_alone(wapmod, orc, torch_cuda):
+    """Jobs submitted with flow_bits = 16 run the precision form in the mix
+    and give the same bits as the same jobs run alone in that form; the
+    footprint reserved for them includes the FP16 pair state."""
+    import oracle as O
+    wap = wapmod
+    specs = [(32, 16, 6), (24, 24, 7), (40, 16, 8)]
+    jobs = [_job(wap, orc, O, n, p, seed) for n, p, seed in specs]
+    alone = [_alone(wap, *j, 1, flow_bits=16) for j in jobs]
+    srv = wap.Server(int(2.5 * max(wap.job_device_bytes(j[0], j[1]) for j in jobs)), workers=2)
+    try:
+        ids = [srv.submit(j[0], j[1], j[2], j[3], outer_iterations=1, flow_bits=16) for j in jobs]
+        for jid in ids:
+            assert srv.wait(jid, 600.0) == wap.WAP_OK
+        for jid, j, (vols, used) in zip(ids, jobs, alone):
+            n = j[0].vol[0]
+            info = srv.info(jid)
+            assert info.device_bytes >= used, (info.device_bytes, used)
+            for f, v in enumerate(vols):
+                assert np.array_equal(srv.result(jid, f, (n, n, n)), v), (jid, f)
+            assert srv.release(jid) == wap.WAP_OK
     finally:
         srv.close()

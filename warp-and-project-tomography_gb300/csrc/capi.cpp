@@ -1020,6 +1020,21 @@ int wap_pass(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
 // ===========================================================================
 // C ABI
 // ===========================================================================
+namespace wap {
+size_t flow_pairs_bytes(const int vol[3], int flow_scales, float flow_eta) {
+  // y: two buffers of 5 pair planes, v: two of 2, u: one of 2 (4 bytes a pair)
+  size_t b = 0;
+  float t_eta = 1.0f;
+  for (int l = 0; l < std::max(flow_scales, 1); ++l) {
+    size_t m = 1;
+    for (int a = 0; a < 3; ++a) m *= (size_t)std::max(1, (int)(vol[a] * t_eta));
+    b += (size_t)4 * (2 * 5 + 2 * 2 + 2) * m;
+    t_eta *= flow_eta;
+  }
+  return b;
+}
+}  // namespace wap
+
 extern "C" {
 
 int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_deg, int device) {
@@ -1596,7 +1611,8 @@ size_t wap_ctx_device_bytes(const wap_ctx *ctx) {
     b += m->want;
   for (const auto &kv : ctx->flow_work) {
     const FlowWork &w = *kv.second;
-    for (const DevMem *m : {&w.va, &w.vb, &w.y, &w.y2, &w.u, &w.kty, &w.kx4prev, &w.warp, &w.acc, &w.err, &w.world})
+    for (const DevMem *m : {&w.va, &w.vb, &w.y, &w.y2, &w.u, &w.kty, &w.kx4prev, &w.warp, &w.acc, &w.err, &w.world,
+                            &w.yh[0], &w.yh[1], &w.vh[0], &w.vh[1], &w.uh})
       b += m->want;
   }
   for (const auto &p : ctx->pyramid)

@@ -26,6 +26,7 @@
 
 #include "wap/wap.h"
 #include "wap/wap_serve.h"
+#include "wap_internal.h"
 
 namespace {
 
@@ -101,6 +102,7 @@ struct wap_server {
   int setup(Job *j) {
     int r = wap_create(&j->ctx, &j->desc.scan, j->angles.data(), device);
     if (r != WAP_OK) return r;
+    if (j->desc.flow_bits == 16 && (r = wap_set_tuning(j->ctx, "flow_bits", 16)) != WAP_OK) return r;
     if ((r = wap_upload_projections(j->ctx, j->projs.data())) != WAP_OK) return r;
     if ((r = wap_level_setup(j->ctx, 0)) != WAP_OK) return r;
     j->nsteps = wap_outer_iteration_nsteps(j->ctx, &j->desc.sched);
@@ -209,6 +211,7 @@ void wap_server_destroy(wap_server *s) {
 
 int wap_server_submit(wap_server *s, const wap_job_desc *job, long long *h_id) {
   if (!s || !job || !h_id || !job->h_angles || !job->h_projs || job->outer_iterations < 1) return WAP_EINVAL;
+  if (job->flow_bits != 0 && job->flow_bits != 32 && job->flow_bits != 16) return WAP_EINVAL;
   const wap_scan_desc &sc = job->scan;
   if (sc.nproj < 1 || sc.det[0] < 5 || sc.det[1] < 5) return WAP_EINVAL;
   std::unique_ptr<Job> j(new Job);
@@ -219,6 +222,8 @@ int wap_server_submit(wap_server *s, const wap_job_desc *job, long long *h_id) {
   j->desc.h_projs = nullptr;
   j->info.device_bytes = wap_job_device_bytes(&sc, &job->sched);
   if (j->info.device_bytes == 0) return WAP_EINVAL;
+  if (job->flow_bits == 16)
+    j->info.device_bytes += wap::flow_pairs_bytes(sc.vol, job->sched.flow_scales, job->sched.flow_eta);
   if (j->info.device_bytes > s->budget) return WAP_ETOOBIG;
   std::lock_guard<std::mutex> lk(s->m);
   j->id = s->next_id++;

@@ -107,4 +107,9 @@ cudaError_t launch_wap_accumulate_batch(const AccJob *d_jobs, int njobs, size_t 
 cudaError_t launch_max_reduce(const float *d, size_t n, unsigned *d_bits, cudaStream_t st);
 float decode_max_bits(unsigned b);
 
+// Device bytes the precision form adds to a job (wap_job_device_bytes counts
+// the FP32 path): the flow solver's FP16 pair state, 64 bytes per voxel of
+// every pyramid level (capi.cpp).
+size_t flow_pairs_bytes(const int vol[3], int flow_scales, float flow_eta);
+
 }  // namespace wap

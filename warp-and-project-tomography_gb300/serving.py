@@ -1,6 +1,9 @@
 """Served form: a seeded Poisson stream of reconstruction jobs of uneven sizes
 through the request loop (wap.Server, include/wap/wap_serve.h).
 
+Jobs run the reference's arithmetic (flow_bits 32) or the precision form
+(flow_bits 16: the flow solver's state as FP16 pairs with its fast arithmetic).
+
 Job mix (the served workload): volume sides drawn from {64, 96, 128, 192,
 256} with weights 0.3/0.25/0.2/0.15/0.1, projection counts from {64, 128,
 192}, detector side 1.5x the volume side, ellipsoid phantoms generated on the
@@ -71,10 +74,17 @@ def make_job(wap, torch, spec):
     return dict(scan=scan, sched=served_schedule(wap, frames), angles=ang, projs=host, n=n)
 
 
-def run(wap, torch, n_jobs=40, rate=20.0, budget_gb=150.0, workers=3, seed=3, max_side=256):
+def run(wap, torch, n_jobs=40, rate=20.0, budget_gb=150.0, workers=3, seed=3, max_side=256, flow_bits=(32,)):
+    """The job stream through the request loop once per entry of flow_bits
+    (the same jobs and arrival times each time); one result dict per entry."""
     specs = job_stream(n_jobs, rate, seed, max_side)
     jobs = [make_job(wap, torch, s) for s in specs]
     torch.cuda.synchronize()
+    return [_serve(wap, specs, jobs, rate, budget_gb, workers, fb) for fb in flow_bits]
+
+
+def _serve(wap, specs, jobs, rate, budget_gb, workers, flow_bits):
+    n_jobs = len(specs)
     budget = int(budget_gb * (1 << 30))
     srv = wap.Server(budget, workers=workers)
     try:
@@ -84,7 +94,8 @@ def run(wap, torch, n_jobs=40, rate=20.0, budget_gb=150.0, workers=3, seed=3, ma
             delay = s["t"] - (time.perf_counter() - start)
             if delay > 0:
                 time.sleep(delay)
-            ids.append(srv.submit(j["scan"], j["sched"], j["angles"], j["projs"], outer_iterations=1))
+            ids.append(srv.submit(j["scan"], j["sched"], j["angles"], j["projs"], outer_iterations=1,
+                                  flow_bits=flow_bits))
         for jid in ids:
             if srv.wait(jid, 3600.0) != wap.WAP_OK:
                 raise wap.WapError("served job %d failed" % jid)
@@ -106,6 +117,7 @@ def run(wap, torch, n_jobs=40, rate=20.0, budget_gb=150.0, workers=3, seed=3, ma
         "peak_reserved_gb": peak / float(1 << 30),
         "sides": {str(k): int(sum(1 for s in specs if s["n"] == k)) for k in SIZES},
         "job": "1 outer iteration, frames = projections/8, 2 CP x 2 SART, 2-level flow x 20 PD its, FP32 BP",
+        "flow_bits": flow_bits,
     }
 
 

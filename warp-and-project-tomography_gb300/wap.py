@@ -77,7 +77,7 @@ class Stats(ctypes.Structure):
 
 class JobDesc(ctypes.Structure):
     _fields_ = [("scan", ScanDesc), ("sched", Schedule), ("outer_iterations", _c_int),
-                ("h_angles", _vp), ("h_projs", _vp)]
+                ("h_angles", _vp), ("h_projs", _vp), ("flow_bits", _c_int)]
 
 
 class JobInfo(ctypes.Structure):
@@ -549,11 +549,11 @@ class Server:
         except Exception:
             pass
 
-    def submit(self, scan, sched, angles, projs, outer_iterations=1):
+    def submit(self, scan, sched, angles, projs, outer_iterations=1, flow_bits=32):
         a = np.ascontiguousarray(angles, np.float64)
         p = np.ascontiguousarray(projs, np.float32)
         d = JobDesc(scan=scan, sched=sched, outer_iterations=int(outer_iterations), h_angles=a.ctypes.data,
-                    h_projs=p.ctypes.data)
+                    h_projs=p.ctypes.data, flow_bits=int(flow_bits))
         jid = ctypes.c_longlong(0)
         r = self.L.wap_server_submit(self.h, ctypes.byref(d), ctypes.byref(jid))
         if r != WAP_OK:
