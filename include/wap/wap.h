@@ -163,9 +163,12 @@ WAP_API int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user);
  * precision form, "flow_bits" = 16 stores the flow solver's dual, flow and
  * linearisation as FP16 pairs during the primal-dual iterations and computes
  * them with fused multiply-adds and hardware reciprocals (FP64 residual sums;
- * grids with nx % 4 == 0, others stay FP32); 32 (the default) is the
- * reference's arithmetic.  Each precision keeps its own autotuned plans.
- * Unknown keys are WAP_EINVAL. */
+ * grids with nx % 4 == 0, others stay FP32), grows the flow pyramid in float
+ * instead of double, and gives the flow solver's and warp-and-project's
+ * warps a fused-multiply-add cubic; the standalone calls (wap_advect,
+ * wap_resize, wap_blur) keep the reference's arithmetic.  32 (the default) is
+ * the reference's arithmetic everywhere.  Each precision keeps its own
+ * autotuned plans.  Unknown keys are WAP_EINVAL. */
 WAP_API int wap_set_tuning(wap_ctx *ctx, const char *key, int value);
 /* The form and z-chunk used for a grid (after its first flow level; before
  * that, the forced values or 0). */

@@ -21,8 +21,17 @@ struct Grid3 {
   float a0[3], a1[3];  // aabb lower/upper per axis
 };
 
-// CImg's cubic kernel, float (CImg.h:13437-13519).
+// CImg's cubic kernel, float (CImg.h:13437-13519).  FAST (the precision
+// form): the same polynomial in Horner form with fused multiply-adds, which
+// rounds differently.
+template <bool FAST>
 __device__ __forceinline__ float cubf(float p, float c, float n, float a, float t) {
+  if (FAST) {
+    const float A = n - p;
+    const float B = __fmaf_rn(2.0f, p, __fmaf_rn(-5.0f, c, __fmaf_rn(4.0f, n, -a)));
+    const float C = __fmaf_rn(3.0f, c - n, a - p);
+    return __fmaf_rn(0.5f * t, __fmaf_rn(__fmaf_rn(C, t, B), t, A), c);
+  }
   return c + 0.5f * (t * (-p + n) + t * t * (2 * p - 5 * c + 4 * n - a) + t * t * t * (-p + 3 * c - 3 * n + a));
 }
 
@@ -66,6 +75,7 @@ __device__ __forceinline__ SamplePoint locate(const Grid3 &G, float px, float py
 }
 
 // sample_image (advection.h:49-88) of one channel at a located point.
+template <bool FAST>
 __device__ __forceinline__ float sample(const float *__restrict__ img, const Grid3 &G, const SamplePoint &s) {
   const int nx = G.n[0], nxy = G.n[0] * G.n[1];
   auto I = [&](int x, int y, int z) { return __ldg(img + (x + nx * y + nxy * z)); };
@@ -88,18 +98,19 @@ __device__ __forceinline__ float sample(const float *__restrict__ img, const Gri
 #pragma unroll
     for (int ky = 0; ky < 4; ++ky) {
       const int y = s.ys[ky];
-      rows[ky] = cubf(I(s.xs[0], y, z), I(s.xs[1], y, z), I(s.xs[2], y, z), I(s.xs[3], y, z), s.dx);
+      rows[ky] = cubf<FAST>(I(s.xs[0], y, z), I(s.xs[1], y, z), I(s.xs[2], y, z), I(s.xs[3], y, z), s.dx);
     }
-    const float pl = cubf(rows[0], rows[1], rows[2], rows[3], s.dy);
+    const float pl = cubf<FAST>(rows[0], rows[1], rows[2], rows[3], s.dy);
     p0 = kz == 0 ? pl : p0;
     p1 = kz == 1 ? pl : p1;
     p2 = kz == 2 ? pl : p2;
     p3 = kz == 3 ? pl : p3;
   }
-  const float c = cubf(p0, p1, p2, p3, s.dz);
+  const float c = cubf<FAST>(p0, p1, p2, p3, s.dz);
   return std_max(mn, std_min(mx, c));
 }
 
+template <bool FAST>
 __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__restrict__ wx,
                                                      const float *__restrict__ wy, const float *__restrict__ wz,
                                                      const AdvectJob *__restrict__ jobs, int nc) {
@@ -116,17 +127,17 @@ __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__
   const float p[3] = {__ldg(wx + i), __ldg(wy + j), __ldg(wz + k)};
   // trace (advection.h:101-115) with dt_trace = -dt.
   SamplePoint s = locate(G, p[0], p[1], p[2]);
-  float v0 = sample(vel, G, s), v1 = sample(vel + nv, G, s), v2 = sample(vel + 2 * nv, G, s);
+  float v0 = sample<FAST>(vel, G, s), v1 = sample<FAST>(vel + nv, G, s), v2 = sample<FAST>(vel + 2 * nv, G, s);
   const float p2[3] = {p[0] + tdt * v0, p[1] + tdt * v1, p[2] + tdt * v2};
   s = locate(G, p2[0], p2[1], p2[2]);
-  v0 = sample(vel, G, s);
-  v1 = sample(vel + nv, G, s);
-  v2 = sample(vel + 2 * nv, G, s);
+  v0 = sample<FAST>(vel, G, s);
+  v1 = sample<FAST>(vel + nv, G, s);
+  v2 = sample<FAST>(vel + 2 * nv, G, s);
   const float p0[3] = {p2[0] - tdt * v0, p2[1] - tdt * v1, p2[2] - tdt * v2};
   const float q[3] = {p2[0] + (p[0] - p0[0]) * 0.5f, p2[1] + (p[1] - p0[1]) * 0.5f, p2[2] + (p[2] - p0[2]) * 0.5f};
   s = locate(G, q[0], q[1], q[2]);
   const size_t o = i + (size_t)G.n[0] * (j + (size_t)G.n[1] * k);
-  for (int c = 0; c < nc; ++c) out[c * nv + o] = sample(src + c * nv, G, s);
+  for (int c = 0; c < nc; ++c) out[c * nv + o] = sample<FAST>(src + c * nv, G, s);
 }
 
 // vol += alpha * adv (double, CImg operator* / operator+=), cut(0, G_Max),
@@ -169,7 +180,7 @@ void world_table(const int dims[3], const float aabb[6], float *h) {
 }
 
 cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d_world, const AdvectJob *d_jobs,
-                          int njobs, int nc, cudaStream_t st) {
+                          int njobs, int nc, cudaStream_t st, bool fast) {
   if (njobs <= 0) return cudaSuccess;
   Grid3 G;
   for (int a = 0; a < 3; ++a) {
@@ -184,7 +195,12 @@ cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d
   for (int j = 0; j < njobs; j += per) {
     const int n = std::min(per, njobs - j);
     const dim3 grid((dims[0] + 31) / 32, (dims[1] + 3) / 4, dims[2] * n);
-    advect_kernel<<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1], d_jobs + j, nc);
+    if (fast)
+      advect_kernel<true><<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1], d_jobs + j,
+                                                  nc);
+    else
+      advect_kernel<false><<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1],
+                                                   d_jobs + j, nc);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

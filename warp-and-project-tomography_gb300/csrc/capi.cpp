@@ -430,7 +430,8 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
   TRY(upload(ctx, ctx->jobs_bp, bp));
   TRY(upload(ctx, ctx->jobs_acc, acc));
   const int n = (int)items.size();
-  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>(), n, 1, ctx->stream));
+  const bool fast = ctx->flow_bits == 16;  // the precision form's warps
+  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>(), n, 1, ctx->stream, fast));
   KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_fp.as<FpJob>(), n, d, W, H, ctx->sd, ctx->scan.alpha,
                     ctx->stream));
   ctx->stats.fp_launches++;
@@ -439,7 +440,7 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
   int mb[3] = {d[0], d[1], d[2]};
   KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_bp.as<BpJob>(), n, mb, d, W, H, ctx->halfW, ctx->halfH,
                      (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha, ctx->gmax, 1, exact, ctx->stream));
-  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + n, n, 1, ctx->stream));
+  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + n, n, 1, ctx->stream, fast));
   ctx->stats.advect_voxels += 2.0 * n * (double)nv;
   ctx->stats.projections += n;
   ctx->stats.backprojections += n;
@@ -471,7 +472,8 @@ int resize_tables(wap_ctx *ctx, int Sin, int Sout, ResizeTables &tb) {
   return WAP_OK;
 }
 
-int do_resize(wap_ctx *ctx, const int dims[3], int nc, const float *src, const int odims[3], float *out) {
+int do_resize(wap_ctx *ctx, const int dims[3], int nc, const float *src, const int odims[3], float *out,
+              bool fast = false) {
   const size_t big = (size_t)std::max(dims[0], odims[0]) * std::max(dims[1], odims[1]) *
                      std::max(dims[2], odims[2]) * nc;
   CU(ctx->rs_a.ensure(sizeof(float) * big));
@@ -491,7 +493,7 @@ int do_resize(wap_ctx *ctx, const int dims[3], int nc, const float *src, const i
     float *dst = (q == na - 1) ? out : ((q % 2 == 0) ? ctx->rs_a.as<float>() : ctx->rs_b.as<float>());
     ResizeTables tb;
     TRY(resize_tables(ctx, cd[a], odims[a], tb));
-    KL(launch_resize_axis(a, cd, nc, odims[a], tb, in, dst, ctx->stream));
+    KL(launch_resize_axis(a, cd, nc, odims[a], tb, in, dst, ctx->stream, fast));
     cd[a] = odims[a];
     in = dst;
   }
@@ -773,7 +775,8 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     aj.vel = vcur;
     std::vector<AdvectJob> ajs{aj};
     TRY(upload(ctx, ctx->jobs_misc, ajs));
-    KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream));
+    KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream,
+                     ctx->flow_bits == 16));
     ctx->stats.advect_voxels += (double)nv;
     KL(launch_linearize(D, w->warp.as<float>(), I1, vcur, w->u.as<float>(), w->kx4prev.as<float>(), ctx->stream));
     if (half) KL(launch_to_pairs(nv, 4, w->u.as<float>(), w->uh.p, ctx->stream));
@@ -923,8 +926,10 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
     CU(cudaEventRecord(lev[l + 1], ctx->stream));
     if (l + 1 < scales) {
       PyramidLevel &N = *ctx->pyramid[l + 1];
-      TRY(do_resize(ctx, P.d, 3, P.v.as<float>(), N.d, N.v.as<float>()));
-      TRY(do_resize(ctx, P.d, 10, P.y.as<float>(), N.d, N.y.as<float>()));
+      // the precision form grows the flow and the dual in float
+      const bool fast = ctx->flow_bits == 16;
+      TRY(do_resize(ctx, P.d, 3, P.v.as<float>(), N.d, N.v.as<float>(), fast));
+      TRY(do_resize(ctx, P.d, 10, P.y.as<float>(), N.d, N.y.as<float>(), fast));
     }
   }
   CU(cudaMemcpyAsync(Vout, fine.v.p, sizeof(float) * 3 * nv, cudaMemcpyDeviceToDevice, ctx->stream));

@@ -31,8 +31,10 @@ struct ResizeTables {
 DericheCoefs deriche_coefs(float sigma);
 cudaError_t launch_deriche(int axis, const int dims[3], int nc, const DericheCoefs &k, const float *in, float *out,
                            cudaStream_t st);
+// fast: growth in float with fused multiply-adds (the precision form); false:
+// CImg's double cubic, bit for bit.
 cudaError_t launch_resize_axis(int axis, const int in_dims[3], int nc, int Sout, const ResizeTables &tb,
-                               const float *in, float *out, cudaStream_t st);
+                               const float *in, float *out, cudaStream_t st, bool fast = false);
 cudaError_t launch_linearize(const FlowDims &D, const float *warp, const float *I1, const float *v, float *u,
                              float *kx4prev, cudaStream_t st);
 cudaError_t launch_pd_fused(const FlowDims &D, int zchunk, const float *yin, float *yout, const float *u,
