@@ -164,3 +164,48 @@ def run_batched(wap, torch, n_jobs=12, workers=4, seed=5, budget_gb=150.0):
     return {"jobs": n_jobs, "workers": workers, "loop_s": t_loop, "batched_s": t_batch,
             "speedup": t_loop / t_batch, "identical": bool(same),
             "sides": sorted(s["n"] for s in specs), "job": "1 outer iteration of the served job schedule"}
+
+
+def run_sequential(wap, torch, n_jobs=3, seed=3, max_side=256, flow_bits=32):
+    """The first n_jobs of the stream run one after another on their own
+    contexts (no request loop): per job its phase times from the library's
+    stats.  Used to attribute a served job's GPU time (e.g. under an ncu
+    launch list)."""
+    out = []
+    for spec in job_stream(n_jobs, 20.0, seed, max_side):
+        j = make_job(wap, torch, spec)
+        ctx = wap.Context(j["scan"], j["angles"])
+        try:
+            ctx.set_tuning("flow_bits", flow_bits)
+            ctx.upload_projections(j["projs"])
+            F = ctx.level_setup(0)
+            t0 = time.perf_counter()
+            st = ctx.outer_iteration(j["sched"])
+            ctx.synchronize()
+            out.append({"side": spec["n"], "projections": spec["nproj"], "frames": F,
+                        "seconds": time.perf_counter() - t0, "cp_sart_s": st.ms_cp / 1e3, "flow_s": st.ms_flow / 1e3,
+                        "wap_s": st.ms_wap / 1e3, "kernel_launches": int(st.kernel_launches)})
+        finally:
+            ctx.close()
+    return out
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    import torch as _torch
+
+    import build as _build
+    import wap as _wap
+
+    ap = argparse.ArgumentParser(description="served jobs one after another, with per-phase times")
+    ap.add_argument("--jobs", type=int, default=3)
+    ap.add_argument("--flow-bits", type=int, default=32)
+    a = ap.parse_args()
+    _build.build()
+    for rec in run_sequential(_wap, _torch, n_jobs=a.jobs, flow_bits=a.flow_bits):
+        print(json.dumps(rec))
