@@ -6,7 +6,8 @@ CUDA-event timing on the library's stream).
 
 Prints one JSON line per kernel: milliseconds per launch and the achieved
 bandwidth against the kernel's algorithmic bytes:
-  pd      one fused primal-dual iteration, 120 B per voxel (y 10+10, v 3+3, u 4)
+  pd      one fused primal-dual iteration, 120 B per voxel (y 10+10, v 3+3, u 4);
+          62 B per voxel in the precision form (--flow-bits 16, FP16 pairs)
   fp      forward projection, V*4 + 16*D bytes (volume once, 4 outputs per pixel)
   bp      voxel-driven backprojection over the ROI, 2*V*4 + 4*D bytes
   advect  one warp of a 1-channel volume by a 3-channel flow, V*(2+3)*4 bytes
@@ -111,7 +112,10 @@ def main():
         st = ctx.stats()
         ms = st.ms_pd / max(st.pd_timed, 1)
         form, zc = ctx.get_tuning([n, n, n])
-        report("pd", ms, 120 * nv, {"iterations": int(its[0]), "form": form, "zchunk": zc})
+        # bytes moved once per iteration: FP32 state 120 B/voxel; the precision
+        # form's FP16 pairs 62 B/voxel (v's third component padded)
+        report("pd", ms, (62 if a.flow_bits == 16 else 120) * nv, {"iterations": int(its[0]), "form": form,
+                                                                    "zchunk": zc})
     ctx.close()
 
 
