@@ -4,6 +4,8 @@ Two libraries live under this directory:
 
 * ``_build/libwaporacle.so`` -- the plain C++/OpenMP restatement of the
   reference's hot path (``wap_oracle.cpp``).  Buildable anywhere with g++.
+  ``_build/libwaporacle64.so`` is the same source with every float quantity
+  in double: the FP64 oracle (``Oracle(fp64=True)``, float64 arrays).
 * ``_ref/libwapref.so`` -- the reference's own sources compiled headless with
   ``ref_harness.cpp`` (``make ref``).  Only buildable where the reference tree
   is present; used to pin the restatement and to generate tests/golden.
@@ -19,6 +21,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libwaporacle.so")
+ORACLE64_SO = os.path.join(HERE, "_build", "libwaporacle64.so")
 REF_SO = os.path.join(HERE, "_ref", "libwapref.so")
 REF_TREE = os.environ.get("WAP_REFERENCE_TREE", "/root/reference")
 
@@ -107,69 +110,78 @@ def _bind(lib, name, res, args):
 
 
 class Oracle:
-    """The restatement (``wap_oracle.cpp``)."""
+    """The restatement (``wap_oracle.cpp``); fp64=True loads its FP64 build,
+    whose arrays and scalars are float64."""
 
-    def __init__(self, path=ORACLE_SO):
+    def __init__(self, path=None, fp64=False):
+        path = path or (ORACLE64_SO if fp64 else ORACLE_SO)
         if not os.path.exists(path):
             build_oracle()
         L = ctypes.CDLL(path)
         S = ctypes.POINTER(Scan)
         self.lib = L
-        _bind(L, "orc_level_frames", _c_int, [_c_int, _c_int, _c_int, _i32, _i32, _f32, ctypes.POINTER(_c_float)])
-        _bind(L, "orc_geometry", None, [S, _c_double, _f32, _f32, _f32, _f32, _f32])
-        _bind(L, "orc_sample_distance", _c_float, [_c_double])
-        _bind(L, "orc_forward", None, [S, _c_double, _f32, _f32, _f32, _f32])
-        _bind(L, "orc_ray_backproject", None, [S, _c_double, _f32, _f32, _f32])
-        _bind(L, "orc_correction", None, [_c_int, _f32, _f32, _f32, ctypes.c_void_p, _c_double, _f32])
-        _bind(L, "orc_bp_voxel", None, [S, _c_double, _f32, _i32, _c_int, _f32])
-        _bind(L, "orc_advect", None, [_i32, _f32, _f32, _f32, _c_int, _c_float, _f32, _c_int])
-        _bind(L, "orc_blur", None, [_i32, _c_int, _c_float, _f32, _f32])
-        _bind(L, "orc_resize", None, [_i32, _c_int, _f32, _i32, _f32])
-        _bind(L, "orc_gradient", None, [_i32, _f32, _f32, _f32, _f32])
-        _bind(L, "orc_flow_level", _c_int, [_i32, _f32, _f32, _f32, _f32, _f32, _f32, _f32, _c_float, _c_float,
-                                            _c_int, _c_int, _f32, _i32, _c_int, _i32])
+        self.fp64 = fp64
+        self.dt = np.float64 if fp64 else np.float32
+        R = _f64 if fp64 else _f32  # arrays of the oracle's arithmetic type
+        cR = _c_double if fp64 else _c_float  # its scalars
+        _bind(L, "orc_level_frames", _c_int, [_c_int, _c_int, _c_int, _i32, _i32, R, ctypes.POINTER(cR)])
+        _bind(L, "orc_geometry", None, [S, _c_double, R, R, R, R, R])
+        _bind(L, "orc_sample_distance", cR, [_c_double])
+        _bind(L, "orc_forward", None, [S, _c_double, R, R, R, R])
+        _bind(L, "orc_ray_backproject", None, [S, _c_double, R, R, R])
+        _bind(L, "orc_correction", None, [_c_int, R, R, R, ctypes.c_void_p, _c_double, R])
+        _bind(L, "orc_bp_voxel", None, [S, _c_double, R, _i32, _c_int, R])
+        _bind(L, "orc_advect", None, [_i32, R, R, R, _c_int, cR, R, _c_int])
+        _bind(L, "orc_blur", None, [_i32, _c_int, cR, R, R])
+        _bind(L, "orc_resize", None, [_i32, _c_int, R, _i32, R])
+        _bind(L, "orc_gradient", None, [_i32, R, R, R, R])
+        _bind(L, "orc_flow_level", _c_int, [_i32, R, R, R, R, R, R, R, cR, cR, _c_int, _c_int, R, _i32, _c_int,
+                                            _i32])
         _bind(L, "orc_last_pd_seconds", _c_double, [])
-        _bind(L, "orc_flow_multiscale", _c_int, [_i32, _f32, _f32, _f32, _c_float, _c_float, _c_int, _c_int,
-                                                 _c_float, _c_float, _c_int, _i32, _c_int, _f32])
-        _bind(L, "orc_sart_prox", None, [S, _f64, _f32, _c_int, _c_int, _c_int, _i32, _f32, _f32])
-        _bind(L, "orc_warp_and_project", None, [S, _f64, _f32, _c_int, _c_float, _f32, _f32, _f32])
-        _bind(L, "orc_cp_dual", None, [S, _i32, _f32, _f32, _f32, _f32])
-        _bind(L, "orc_cp_primal", None, [S, _i32, _c_int, ctypes.c_void_p, _f32, _f32, _f32, _f32])
-        _bind(L, "orc_cp_overrelax", None, [_i32, _i32, _f32, _f32, _f32])
-        _bind(L, "orc_outer_iteration", _c_int, [S, ctypes.POINTER(Schedule), _f64, _f32, _c_int, _f32, _f32, _f32,
-                                                 _f32, _f32, _f32, ctypes.POINTER(_c_int)])
-        _bind(L, "orc_cg_screened_laplacian", _c_int, [_i32, _c_float, _c_float, _f32, _f32, _c_float, _c_int,
-                                                       _c_float, _c_int])
+        _bind(L, "orc_flow_multiscale", _c_int, [_i32, R, R, R, cR, cR, _c_int, _c_int, cR, cR, _c_int, _i32,
+                                                 _c_int, R])
+        _bind(L, "orc_sart_prox", None, [S, _f64, R, _c_int, _c_int, _c_int, _i32, R, R])
+        _bind(L, "orc_warp_and_project", None, [S, _f64, R, _c_int, cR, R, R, R])
+        _bind(L, "orc_cp_dual", None, [S, _i32, R, R, R, R])
+        _bind(L, "orc_cp_primal", None, [S, _i32, _c_int, ctypes.c_void_p, R, R, R, R])
+        _bind(L, "orc_cp_overrelax", None, [_i32, _i32, R, R, R])
+        _bind(L, "orc_outer_iteration", _c_int, [S, ctypes.POINTER(Schedule), _f64, R, _c_int, R, R, R, R, R, R,
+                                                 ctypes.POINTER(_c_int)])
+        _bind(L, "orc_cg_screened_laplacian", _c_int, [_i32, cR, cR, R, R, cR, _c_int, cR, _c_int])
+
+    def arr(self, x):
+        """x as a contiguous array of the oracle's arithmetic type."""
+        return np.ascontiguousarray(x, self.dt)
 
     # -- thin numpy wrappers ------------------------------------------------
     def level_frames(self, nframes_cli, nproj, level):
         st = np.zeros(130, np.int32)
         en = np.zeros(130, np.int32)
-        ft = np.zeros(130, np.float32)
-        tu = _c_float()
+        ft = np.zeros(130, self.dt)
+        tu = _c_double() if self.fp64 else _c_float()
         nf = self.lib.orc_level_frames(nframes_cli, nproj, level, st, en, ft, ctypes.byref(tu))
         return nf, st[:nf].copy(), en[:nf].copy(), ft[:nf].copy(), tu.value
 
     def geometry(self, scan, angle):
-        out = [np.zeros(16, np.float32) for _ in range(4)] + [np.zeros(4, np.float32)]
+        out = [np.zeros(16, self.dt) for _ in range(4)] + [np.zeros(4, self.dt)]
         self.lib.orc_geometry(ctypes.byref(scan), angle, *out)
         return out
 
     def forward(self, scan, angle, vol):
         W, H = scan.det
-        img, ln, wt = (np.zeros((H, W), np.float32) for _ in range(3))
-        self.lib.orc_forward(ctypes.byref(scan), angle, np.ascontiguousarray(vol, np.float32), img, ln, wt)
+        img, ln, wt = (np.zeros((H, W), self.dt) for _ in range(3))
+        self.lib.orc_forward(ctypes.byref(scan), angle, self.arr(vol), img, ln, wt)
         return img, ln, wt
 
     def ray_backproject(self, scan, angle, corr):
         shp = tuple(reversed(list(scan.vol)))
-        c = np.zeros(shp, np.float32)
-        w = np.zeros(shp, np.float32)
-        self.lib.orc_ray_backproject(ctypes.byref(scan), angle, np.ascontiguousarray(corr, np.float32), c, w)
+        c = np.zeros(shp, self.dt)
+        w = np.zeros(shp, self.dt)
+        self.lib.orc_ray_backproject(ctypes.byref(scan), angle, self.arr(corr), c, w)
         return c, w
 
     def correction(self, p, ax, ln, dual, alpha):
-        c = np.zeros_like(p, dtype=np.float32)
+        c = np.zeros_like(p, dtype=self.dt)
         dptr = dual.ctypes.data_as(ctypes.c_void_p) if dual is not None else None
         self.lib.orc_correction(p.size, p, ax, ln, dptr, alpha, c)
         return c
@@ -180,44 +192,44 @@ class Oracle:
 
     def advect(self, dims, aabb, vel, src, dt, threads=0):
         nc = src.size // int(np.prod(dims))
-        out = np.zeros_like(src, dtype=np.float32)
-        self.lib.orc_advect(np.asarray(dims, np.int32), np.asarray(aabb, np.float32), vel, src, nc, dt, out, threads)
+        out = np.zeros_like(src, dtype=self.dt)
+        self.lib.orc_advect(np.asarray(dims, np.int32), self.arr(aabb), vel, src, nc, dt, out, threads)
         return out
 
     def blur(self, dims, src, sigma):
         nc = src.size // int(np.prod(dims))
-        out = np.zeros_like(src, dtype=np.float32)
+        out = np.zeros_like(src, dtype=self.dt)
         self.lib.orc_blur(np.asarray(dims, np.int32), nc, sigma, src, out)
         return out
 
     def resize(self, dims, src, odims):
         nc = src.size // int(np.prod(dims))
-        out = np.zeros((nc, odims[2], odims[1], odims[0]), np.float32)
+        out = np.zeros((nc, odims[2], odims[1], odims[0]), self.dt)
         self.lib.orc_resize(np.asarray(dims, np.int32), nc, src, np.asarray(odims, np.int32), out)
         return out
 
     def gradient(self, dims, src):
-        g = [np.zeros_like(src, dtype=np.float32) for _ in range(3)]
+        g = [np.zeros_like(src, dtype=self.dt) for _ in range(3)]
         self.lib.orc_gradient(np.asarray(dims, np.int32), src, *g)
         return g
 
     def flow_level(self, dims, I1, I2, V, Y1, Y2, Y3, Y4, tol, lam, iters, nwarps, aabb, roi, deterministic=1):
         its = np.zeros(max(nwarps, 1), np.int32)
         tot = self.lib.orc_flow_level(np.asarray(dims, np.int32), I1, I2, V, Y1, Y2, Y3, Y4, tol, lam, iters,
-                                      nwarps, np.asarray(aabb, np.float32), np.asarray(roi, np.int32),
+                                      nwarps, self.arr(aabb), np.asarray(roi, np.int32),
                                       deterministic, its)
         return tot, its
 
     def flow_multiscale(self, dims, I1, I2, V0, tol, lam, iters, nwarps, eta, sigma, scales, cut6,
                         deterministic=1):
-        out = np.zeros_like(V0, dtype=np.float32)
+        out = np.zeros_like(V0, dtype=self.dt)
         tot = self.lib.orc_flow_multiscale(np.asarray(dims, np.int32), I1, I2, V0, tol, lam, iters, nwarps, eta,
                                            sigma, scales, np.asarray(cut6, np.int32), deterministic, out)
         return out, tot
 
     def sart_prox(self, scan, angles, projs, pstart, pend, nb_sart, box, vol):
         W, H = scan.det
-        dual = np.zeros((scan.nproj, H, W), np.float32)
+        dual = np.zeros((scan.nproj, H, W), self.dt)
         self.lib.orc_sart_prox(ctypes.byref(scan), angles, projs, pstart, pend, nb_sart, np.asarray(box, np.int32),
                                vol, dual)
         return vol, dual

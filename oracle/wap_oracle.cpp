@@ -3,7 +3,7 @@
 // A restatement of the reference's CPU algorithm in plain C++/OpenMP.  It is
 // the checker for the GPU product (tests/, smoke(), bench.py's CPU baseline)
 // and is never linked into the product.  Compiled with -ffp-contract=off so
-// every float operation rounds where the reference's does.  The
+// every real operation rounds where the reference's does.  The
 // parity-defining choices for the reference's undefined spots are:
 //   * one PSART dual row per projection id, zeroed per SART call;
 //   * imROI == 1 (m_roi is zero when SetData builds it);
@@ -23,11 +23,14 @@
 
 namespace {
 
+// float or double: see orc_real in wap_oracle.h.
+typedef orc_real real;
+
 // ---------------------------------------------------------------------------
-// 4x4 float matrices, column-major (Matrix4x4.h / Matrix4x4.cpp semantics)
+// 4x4 real matrices, column-major (Matrix4x4.h / Matrix4x4.cpp semantics)
 // ---------------------------------------------------------------------------
 struct M4 {
-  float e[16];
+  real e[16];
 };
 
 M4 m4_identity() {
@@ -47,28 +50,28 @@ M4 m4_mul(const M4 &A, const M4 &B) {
 }
 
 // Matrix4x4.h operator*(Mat, Vec).
-void m4_vec(const float *M, const float v[4], float out[4]) {
+void m4_vec(const real *M, const real v[4], real out[4]) {
   for (int r = 0; r < 4; ++r) out[r] = M[r] * v[0] + M[4 + r] * v[1] + M[8 + r] * v[2] + M[12 + r] * v[3];
 }
 
-inline float det3(float a, float b, float c, float d, float e, float f, float g, float h, float i) {
+inline real det3(real a, real b, real c, real d, real e, real f, real g, real h, real i) {
   return a * e * i + b * f * g + c * d * h - c * e * g - a * f * h - b * d * i;
 }
 
 // Cofactor inverse, Matrix4x4.cpp:80-135 (returns unchanged when singular).
 void m4_inverse(M4 &m) {
-  float *e = m.e;
-  float a1 = e[0], b1 = e[1], c1 = e[2], d1 = e[3];
-  float a2 = e[4], b2 = e[5], c2 = e[6], d2 = e[7];
-  float a3 = e[8], b3 = e[9], c3 = e[10], d3 = e[11];
-  float a4 = e[12], b4 = e[13], c4 = e[14], d4 = e[15];
-  float det1 = det3(b2, b3, b4, c2, c3, c4, d2, d3, d4);
-  float det2 = det3(a2, a3, a4, c2, c3, c4, d2, d3, d4);
-  float det3_ = det3(a2, a3, a4, b2, b3, b4, d2, d3, d4);
-  float det4 = det3(a2, a3, a4, b2, b3, b4, c2, c3, c4);
-  float det = a1 * det1 - b1 * det2 + c1 * det3_ - d1 * det4;
+  real *e = m.e;
+  real a1 = e[0], b1 = e[1], c1 = e[2], d1 = e[3];
+  real a2 = e[4], b2 = e[5], c2 = e[6], d2 = e[7];
+  real a3 = e[8], b3 = e[9], c3 = e[10], d3 = e[11];
+  real a4 = e[12], b4 = e[13], c4 = e[14], d4 = e[15];
+  real det1 = det3(b2, b3, b4, c2, c3, c4, d2, d3, d4);
+  real det2 = det3(a2, a3, a4, c2, c3, c4, d2, d3, d4);
+  real det3_ = det3(a2, a3, a4, b2, b3, b4, d2, d3, d4);
+  real det4 = det3(a2, a3, a4, b2, b3, b4, c2, c3, c4);
+  real det = a1 * det1 - b1 * det2 + c1 * det3_ - d1 * det4;
   if (det == 0.0f) return;
-  float invdet = 1.0f / det;
+  real invdet = 1.0f / det;
   e[0] = det1 * invdet;
   e[4] = -det2 * invdet;
   e[8] = det3_ * invdet;
@@ -97,12 +100,12 @@ inline auto mac_max(A a, B b) {
   return (a > b) ? a : b;
 }
 // std::min / std::max argument order (used by advection.h, optical_flow.h).
-inline float std_min(float a, float b) { return (b < a) ? b : a; }
-inline float std_max(float a, float b) { return (a < b) ? b : a; }
+inline real std_min(real a, real b) { return (b < a) ? b : a; }
+inline real std_max(real a, real b) { return (a < b) ? b : a; }
 
 struct ProjGeom {
   M4 p2m, m2v, mv, v2m, mvv2m;
-  float eye[4];
+  real eye[4];
 };
 
 // PSART::RotateVolume + Scene::_calculateCamera/_calculateMatrix +
@@ -112,39 +115,39 @@ ProjGeom make_geometry(const orc_scan *s, double angle_deg) {
   ProjGeom g;
   // WaP_Tomo.cpp:1775-1791: quaternion about +y (IS_COUNTERCLOCK = 1).
   double angle = angle_deg * 3.1415926 / 180;
-  float v[4] = {0.0f, 1.0f, 0.0f, 0.0f};
-  double length = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);  // sqrtf: all operands float
-  float sc = (float)(1.0f / length);
+  real v[4] = {0.0f, 1.0f, 0.0f, 0.0f};
+  double length = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);  // sqrtf: all operands real
+  real sc = (real)(1.0f / length);
   for (int i = 0; i < 4; ++i) v[i] *= sc;
-  float qang = (float)(length * angle);
+  real qang = (real)(length * angle);
   // Quaternion.cpp:7-40
-  float ax = v[0], ay = v[1], az = v[2];
-  float qlen = std::sqrt(ax * ax + ay * ay + az * az);
-  float qx, qy, qz, qw;
+  real ax = v[0], ay = v[1], az = v[2];
+  real qlen = std::sqrt(ax * ax + ay * ay + az * az);
+  real qx, qy, qz, qw;
   if (0.0f == qlen) {
     qw = 1.0f;
     qx = qy = qz = 0.0f;
   } else {
-    float lenInv = 1.0f / qlen;
-    float xx = ax * lenInv, yy = ay * lenInv, zz = az * lenInv;
-    float rad = qang / 2;
+    real lenInv = 1.0f / qlen;
+    real xx = ax * lenInv, yy = ay * lenInv, zz = az * lenInv;
+    real rad = qang / 2;
     qw = std::cos(rad);
-    float scale = std::sin(rad);
+    real scale = std::sin(rad);
     qx = xx * scale;
     qy = yy * scale;
     qz = zz * scale;
   }
   // q * identity (Quaternion.h:269-279 with m_OldRotation = identity).
-  float ow = 1.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
-  float rw = qw * ow - qx * ox - qy * oy - qz * oz;
-  float rx = qw * ox + qx * ow + qy * oz - qz * oy;
-  float ry = qw * oy + qy * ow + qz * ox - qx * oz;
-  float rz = qw * oz + qz * ow + qx * oy - qy * ox;
+  real ow = 1.0f, ox = 0.0f, oy = 0.0f, oz = 0.0f;
+  real rw = qw * ow - qx * ox - qy * oy - qz * oz;
+  real rx = qw * ox + qx * ow + qy * oz - qz * oy;
+  real ry = qw * oy + qy * ow + qz * ox - qx * oz;
+  real rz = qw * oz + qz * ow + qx * oy - qy * ox;
   // Quaternion::ToMatrix (Quaternion.h:46-72).
   M4 R = m4_identity();
   {
-    float x = rx, y = ry, z = rz, w = rw;
-    float *m = R.e;
+    real x = rx, y = ry, z = rz, w = rw;
+    real *m = R.e;
     m[0] = 1.0f - 2.0f * (y * y + z * z);
     m[1] = 2.0f * (x * y + z * w);
     m[2] = 2.0f * (z * x - y * w);
@@ -161,14 +164,14 @@ ProjGeom make_geometry(const orc_scan *s, double angle_deg) {
     m[15] = 1.0f;
   }
   // Scene members (floats) from the PSART constructor (WaP_Tomo.cpp:251-286).
-  float sid = (float)s->sid, sdd = (float)s->sdd;
-  float tr0 = (float)(-s->oxyz[0]), tr2 = (float)(+s->oxyz[1]), tr1 = (float)(-s->oxyz[2]);
+  real sid = (real)s->sid, sdd = (real)s->sdd;
+  real tr0 = (real)(-s->oxyz[0]), tr2 = (real)(+s->oxyz[1]), tr1 = (real)(-s->oxyz[2]);
   double halfW = (s->det[0] - 1) * s->ds * 0.5f;
   double halfH = (s->det[1] - 1) * s->ds * 0.5f;
   // Scene::_calculateCamera (Scene.cpp:65-127).
-  float zbase = -1 * sid;
-  float nearp = sdd;
-  float farp = (float)10000.0;
+  real zbase = -1 * sid;
+  real nearp = sdd;
+  real farp = (real)10000.0;
   // Scene::_calculateMatrix (Scene.cpp:163-189).
   M4 T = m4_identity();
   T.e[12] = tr0;
@@ -177,10 +180,10 @@ ProjGeom make_geometry(const orc_scan *s, double angle_deg) {
   M4 S = m4_identity();
   M4 view = m4_mul(m4_mul(T, S), R);
   M4 proj;
-  proj.e[0] = (float)(nearp / halfW);
+  proj.e[0] = (real)(nearp / halfW);
   proj.e[1] = proj.e[2] = proj.e[3] = 0.0f;
   proj.e[4] = 0.0f;
-  proj.e[5] = (float)(nearp / halfH);
+  proj.e[5] = (real)(nearp / halfH);
   proj.e[6] = proj.e[7] = proj.e[8] = proj.e[9] = 0.0f;
   proj.e[10] = -(farp + nearp) / (farp - nearp);
   proj.e[11] = -1.0f;
@@ -188,8 +191,8 @@ ProjGeom make_geometry(const orc_scan *s, double angle_deg) {
   proj.e[14] = -2.0f * farp * nearp / (farp - nearp);
   proj.e[15] = 0.0f;
   // TypicalRayProducer::SetVolSize / _calculateMatrix (TypicalRayProducer.cpp:118-232).
-  float sp = (float)s->vs;
-  float volsize[3] = {(s->vol[0] - 1) * sp, (s->vol[1] - 1) * sp, (s->vol[2] - 1) * sp};
+  real sp = (real)s->vs;
+  real volsize[3] = {(s->vol[0] - 1) * sp, (s->vol[1] - 1) * sp, (s->vol[2] - 1) * sp};
   M4 Tv = m4_identity();
   Tv.e[12] = -volsize[0] * 0.5f;
   Tv.e[13] = -volsize[1] * 0.5f;
@@ -232,9 +235,9 @@ ProjGeom make_geometry(const orc_scan *s, double angle_deg) {
 // Forward projector
 // ---------------------------------------------------------------------------
 struct Vol {
-  const float *d;
+  const real *d;
   int n[3];
-  float at(int x, int y, int z) const {  // SingleScalarVolume.core.h:66-83
+  real at(int x, int y, int z) const {  // SingleScalarVolume.core.h:66-83
     x = mac_max(mac_min(x, n[0] - 1), 0);
     y = mac_max(mac_min(y, n[1] - 1), 0);
     z = mac_max(mac_min(z, n[2] - 1), 0);
@@ -243,19 +246,19 @@ struct Vol {
 };
 
 struct Splat {
-  float *contrib, *weight;
-  float corr;
+  real *contrib, *weight;
+  real corr;
 };
 
 // T_VolumeAccess::GetScalarValue(Vector4) (SingleScalarVolume.core.h:99-202).
-inline float sample_trilinear(const Vol &v, float p0, float p1, float p2, float &sumw, Splat *splat) {
-  float pos[3] = {p0, p1, p2};
-  for (int a = 0; a < 3; ++a) pos[a] = mac_max(mac_min(pos[a], (float)(v.n[a] - 1)), 0.0f);
+inline real sample_trilinear(const Vol &v, real p0, real p1, real p2, real &sumw, Splat *splat) {
+  real pos[3] = {p0, p1, p2};
+  for (int a = 0; a < 3; ++a) pos[a] = mac_max(mac_min(pos[a], (real)(v.n[a] - 1)), 0.0f);
   int ip[3] = {(int)pos[0], (int)pos[1], (int)pos[2]};
   if (splat) {
-    float t0 = pos[0] - ip[0], t1 = pos[1] - ip[1], t2 = pos[2] - ip[2];
-    float M0 = 1.0f - t0, M1 = 1.0f - t1, M2 = 1.0f - t2;
-    float w[8] = {M0 * M1 * M2, t0 * M1 * M2, M0 * t1 * M2, t0 * t1 * M2,
+    real t0 = pos[0] - ip[0], t1 = pos[1] - ip[1], t2 = pos[2] - ip[2];
+    real M0 = 1.0f - t0, M1 = 1.0f - t1, M2 = 1.0f - t2;
+    real w[8] = {M0 * M1 * M2, t0 * M1 * M2, M0 * t1 * M2, t0 * t1 * M2,
                   M0 * M1 * t2, t0 * M1 * t2, M0 * t1 * t2, t0 * t1 * t2};
     // Taps past the last voxel carry weight 0 (pos is clamped to dim-1).
     for (int c = 0; c < 8; ++c) {
@@ -267,13 +270,13 @@ inline float sample_trilinear(const Vol &v, float p0, float p1, float p2, float 
     }
     return 0.0f;
   }
-  float f2 = pos[0] - ip[0];
-  float f1 = 1.0f - f2;
+  real f2 = pos[0] - ip[0];
+  real f1 = 1.0f - f2;
   sumw += 1.0f;
-  float a = v.at(ip[0], ip[1], ip[2]) * f1 + v.at(ip[0] + 1, ip[1], ip[2]) * f2;
-  float b = v.at(ip[0], ip[1] + 1, ip[2]) * f1 + v.at(ip[0] + 1, ip[1] + 1, ip[2]) * f2;
-  float c = v.at(ip[0], ip[1], ip[2] + 1) * f1 + v.at(ip[0] + 1, ip[1], ip[2] + 1) * f2;
-  float d = v.at(ip[0], ip[1] + 1, ip[2] + 1) * f1 + v.at(ip[0] + 1, ip[1] + 1, ip[2] + 1) * f2;
+  real a = v.at(ip[0], ip[1], ip[2]) * f1 + v.at(ip[0] + 1, ip[1], ip[2]) * f2;
+  real b = v.at(ip[0], ip[1] + 1, ip[2]) * f1 + v.at(ip[0] + 1, ip[1] + 1, ip[2]) * f2;
+  real c = v.at(ip[0], ip[1], ip[2] + 1) * f1 + v.at(ip[0] + 1, ip[1], ip[2] + 1) * f2;
+  real d = v.at(ip[0], ip[1] + 1, ip[2] + 1) * f1 + v.at(ip[0] + 1, ip[1] + 1, ip[2] + 1) * f2;
   f2 = pos[1] - ip[1];
   f1 = 1.0f - f2;
   a = a * f1 + b * f2;
@@ -284,17 +287,17 @@ inline float sample_trilinear(const Vol &v, float p0, float p1, float p2, float 
 }
 
 // CastingRay with block size == volume size (RayCaster.core.h:42-188,191-207).
-float cast_ray(const Vol &v, const float vz[4], const float vu[4], float tnear, float tfar, float sd, float &sumw,
+real cast_ray(const Vol &v, const real vz[4], const real vu[4], real tnear, real tfar, real sd, real &sumw,
                Splat *splat) {
-  float density = 0.0f;
-  float t1 = tnear;
-  float pos1[4];
+  real density = 0.0f;
+  real t1 = tnear;
+  real pos1[4];
   for (int a = 0; a < 4; ++a) pos1[a] = vz[a] + vu[a] * t1;
-  float step[4];
+  real step[4];
   for (int a = 0; a < 4; ++a) step[a] = vu[a] * sd;
-  float s1 = sample_trilinear(v, pos1[0], pos1[1], pos1[2], sumw, splat);
+  real s1 = sample_trilinear(v, pos1[0], pos1[1], pos1[2], sumw, splat);
   density += s1 * sd;
-  float tMax[3], tDelta[3] = {0.0f, 0.0f, 0.0f};
+  real tMax[3], tDelta[3] = {0.0f, 0.0f, 0.0f};
   for (int a = 0; a < 3; ++a) {
     int bs = v.n[a];
     int blk;
@@ -312,10 +315,10 @@ float cast_ray(const Vol &v, const float vz[4], const float vu[4], float tnear, 
     }
   }
   while (t1 < tfar) {
-    float tb = mac_min(mac_min(tMax[0], tMax[1]), tMax[2]);
+    real tb = mac_min(mac_min(tMax[0], tMax[1]), tMax[2]);
     if (tb > tfar) tb = tfar;
-    float t = std::ceil((t1 - tnear) / sd) * sd + tnear;
-    float pos[4];
+    real t = std::ceil((t1 - tnear) / sd) * sd + tnear;
+    real pos[4];
     for (int a = 0; a < 4; ++a) pos[a] = vz[a] + vu[a] * t;
     while (t < tb) {
       density += sample_trilinear(v, pos[0], pos[1], pos[2], sumw, splat) * sd;
@@ -335,26 +338,26 @@ float cast_ray(const Vol &v, const float vz[4], const float vu[4], float tnear, 
 }
 
 // ProduceRay (TypicalRayProducer.core.h:32-120).
-inline void produce_ray(const ProjGeom &g, const int dims[3], float px, float py, float vz[4], float vu[4],
-                        float &tnear, float &tfar) {
-  float pin[4] = {px, py, 0.0f, 1.0f};
-  float mp[4];
+inline void produce_ray(const ProjGeom &g, const int dims[3], real px, real py, real vz[4], real vu[4],
+                        real &tnear, real &tfar) {
+  real pin[4] = {px, py, 0.0f, 1.0f};
+  real mp[4];
   m4_vec(g.p2m.e, pin, mp);
-  float inv = 1.0f / mp[3];
+  real inv = 1.0f / mp[3];
   for (int a = 0; a < 4; ++a) mp[a] *= inv;
-  float dir[4];
+  real dir[4];
   for (int a = 0; a < 4; ++a) dir[a] = mp[a] - g.eye[a];
-  float li = 1.0f / std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+  real li = 1.0f / std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
   dir[0] *= li;
   dir[1] *= li;
   dir[2] *= li;
   m4_vec(g.m2v.e, g.eye, vz);
   m4_vec(g.m2v.e, dir, vu);
-  float tmn[3], tmx[3];
+  real tmn[3], tmx[3];
   for (int a = 0; a < 3; ++a) {
-    float lo = 0.0f, hi = (float)(dims[a] - 1);
-    float t1 = (lo - vz[a]) / vu[a];
-    float t2 = (hi - vz[a]) / vu[a];
+    real lo = 0.0f, hi = (real)(dims[a] - 1);
+    real t1 = (lo - vz[a]) / vu[a];
+    real t2 = (hi - vz[a]) / vu[a];
     tmn[a] = mac_min(t1, t2);
     tmx[a] = mac_max(t1, t2);
   }
@@ -370,13 +373,13 @@ void set_threads(int t) {
 // ---------------------------------------------------------------------------
 // Bicubic backprojection helpers (WaP_Tomo.cpp:208-222, double arithmetic)
 // ---------------------------------------------------------------------------
-inline float cubic_interp(const float p[4], float x) {
+inline real cubic_interp(const real p[4], real x) {
   return p[1] + 0.5 * x * (p[2] - p[0] + x * (2.0 * p[0] - 5.0 * p[1] + 4.0 * p[2] - p[3] +
                                                x * (3.0 * (p[1] - p[2]) + p[3] - p[0])));
 }
 
-inline float bicubic_interp(float p[4][4], float x, float y) {
-  float arr[4];
+inline real bicubic_interp(real p[4][4], real x, real y) {
+  real arr[4];
   arr[0] = cubic_interp(p[0], y);
   arr[1] = cubic_interp(p[1], y);
   arr[2] = cubic_interp(p[2], y);
@@ -388,28 +391,28 @@ inline float bicubic_interp(float p[4][4], float x, float y) {
 // Advection (advection.h) with CImg's _cubic_atXYZ (CImg.h:13429-13524)
 // ---------------------------------------------------------------------------
 struct Img {
-  const float *d;
+  const real *d;
   int n[3];
-  float operator()(int x, int y, int z) const { return d[x + (size_t)n[0] * (y + (size_t)n[1] * z)]; }
+  real operator()(int x, int y, int z) const { return d[x + (size_t)n[0] * (y + (size_t)n[1] * z)]; }
 };
 
-inline float cimg_cut(float v, float lo, float hi) { return v < lo ? lo : (v > hi ? hi : v); }
+inline real cimg_cut(real v, real lo, real hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-inline float cub(float p, float c, float n, float a, float t) {
+inline real cub(real p, real c, real n, real a, real t) {
   return c + 0.5f * (t * (-p + n) + t * t * (2 * p - 5 * c + 4 * n - a) + t * t * t * (-p + 3 * c - 3 * n + a));
 }
 
-float cubic_atXYZ(const Img &I, float fx, float fy, float fz) {
-  const float nfx = cimg_cut(fx, 0, I.n[0] - 1), nfy = cimg_cut(fy, 0, I.n[1] - 1), nfz = cimg_cut(fz, 0, I.n[2] - 1);
+real cubic_atXYZ(const Img &I, real fx, real fy, real fz) {
+  const real nfx = cimg_cut(fx, 0, I.n[0] - 1), nfy = cimg_cut(fy, 0, I.n[1] - 1), nfz = cimg_cut(fz, 0, I.n[2] - 1);
   const int x = (int)nfx, y = (int)nfy, z = (int)nfz;
-  const float dx = nfx - x, dy = nfy - y, dz = nfz - z;
+  const real dx = nfx - x, dy = nfy - y, dz = nfz - z;
   const int px = x - 1 < 0 ? 0 : x - 1, nx = dx > 0 ? x + 1 : x, ax = x + 2 >= I.n[0] ? I.n[0] - 1 : x + 2;
   const int py = y - 1 < 0 ? 0 : y - 1, ny = dy > 0 ? y + 1 : y, ay = y + 2 >= I.n[1] ? I.n[1] - 1 : y + 2;
   const int pz = z - 1 < 0 ? 0 : z - 1, nz = dz > 0 ? z + 1 : z, az = z + 2 >= I.n[2] ? I.n[2] - 1 : z + 2;
   const int xs[4] = {px, x, nx, ax}, ys[4] = {py, y, ny, ay}, zs[4] = {pz, z, nz, az};
-  float planes[4];
+  real planes[4];
   for (int kz = 0; kz < 4; ++kz) {
-    float rows[4];
+    real rows[4];
     for (int ky = 0; ky < 4; ++ky)
       rows[ky] = cub(I(xs[0], ys[ky], zs[kz]), I(xs[1], ys[ky], zs[kz]), I(xs[2], ys[ky], zs[kz]),
                      I(xs[3], ys[ky], zs[kz]), dx);
@@ -419,23 +422,23 @@ float cubic_atXYZ(const Img &I, float fx, float fy, float fz) {
 }
 
 // advection::sample_image (advection.h:49-88).
-float sample_image(const int dims[3], const float aabb[6], const Img &I, const float p[3]) {
-  float g[3];
+real sample_image(const int dims[3], const real aabb[6], const Img &I, const real p[3]) {
+  real g[3];
   for (int a = 0; a < 3; ++a)
-    g[a] = (float)((double)((float)dims[a] * (p[a] - aabb[2 * a]) / (aabb[2 * a + 1] - aabb[2 * a])) - 0.5);
-  for (int a = 0; a < 3; ++a) g[a] = std_max(1.0f, std_min((float)(dims[a] - 2), g[a]));
+    g[a] = (real)((double)((real)dims[a] * (p[a] - aabb[2 * a]) / (aabb[2 * a + 1] - aabb[2 * a])) - 0.5);
+  for (int a = 0; a < 3; ++a) g[a] = std_max(1.0f, std_min((real)(dims[a] - 2), g[a]));
   int ix = (int)g[0], iy = (int)g[1], iz = (int)g[2];
-  float mn = I(ix, iy, iz), mx = mn;
+  real mn = I(ix, iy, iz), mx = mn;
   const int o[7][3] = {{1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
   for (int q = 0; q < 7; ++q) {
-    float v = I(ix + o[q][0], iy + o[q][1], iz + o[q][2]);
+    real v = I(ix + o[q][0], iy + o[q][1], iz + o[q][2]);
     mn = std_min(mn, v);
     mx = std_max(mx, v);
   }
   return std_max(mn, std_min(mx, cubic_atXYZ(I, g[0], g[1], g[2])));
 }
 
-void sample_velocity(const int dims[3], const float aabb[6], const float *vel, const float p[3], float v[3]) {
+void sample_velocity(const int dims[3], const real aabb[6], const real *vel, const real p[3], real v[3]) {
   size_t nv = (size_t)dims[0] * dims[1] * dims[2];
   for (int c = 0; c < 3; ++c) {
     Img I{vel + c * nv, {dims[0], dims[1], dims[2]}};
@@ -448,13 +451,13 @@ void sample_velocity(const int dims[3], const float aabb[6], const float *vel, c
 extern "C" {
 
 // VolumeData::ReadStructuredFile (VolumeData.cpp:133-210): nf, timeunit, windows.
-int orc_level_frames(int nframes_cli, int nproj, int level, int *start, int *end, float *ftime, float *tunit) {
+int orc_level_frames(int nframes_cli, int nproj, int level, int *start, int *end, real *ftime, real *tunit) {
   int factor = 1 << level;
   int nf = std::min(nframes_cli * factor, 130);
-  float timeunit = (float)((float)nproj / (float)nf);
-  float baseNo = 3;
+  real timeunit = (real)((real)nproj / (real)nf);
+  real baseNo = 3;
   for (int i = 0; i < nf; ++i) {
-    float t = timeunit * i;
+    real t = timeunit * i;
     if (ftime) ftime[i] = t;
     if (start) start[i] = std::max(0, (int)(t - baseNo));
     if (end) end[i] = std::min((int)(t + baseNo), nproj - 1);
@@ -463,36 +466,36 @@ int orc_level_frames(int nframes_cli, int nproj, int level, int *start, int *end
   return nf;
 }
 
-float orc_sample_distance(double vs) {
-  // PSART::SetData (WaP_Tomo.cpp:380): sqrt of the float sum of squares / 2.
-  float sp = (float)vs;
+real orc_sample_distance(double vs) {
+  // PSART::SetData (WaP_Tomo.cpp:380): sqrt of the real sum of squares / 2.
+  real sp = (real)vs;
   return std::sqrt(sp * sp + sp * sp + sp * sp) / 2;
 }
 
-void orc_geometry(const orc_scan *s, double angle_deg, float p2m[16], float m2v[16], float mv[16], float v2m[16],
-                  float eye[4]) {
+void orc_geometry(const orc_scan *s, double angle_deg, real p2m[16], real m2v[16], real mv[16], real v2m[16],
+                  real eye[4]) {
   ProjGeom g = make_geometry(s, angle_deg);
-  std::memcpy(p2m, g.p2m.e, 64);
-  std::memcpy(m2v, g.m2v.e, 64);
-  std::memcpy(mv, g.mv.e, 64);
-  std::memcpy(v2m, g.v2m.e, 64);
-  std::memcpy(eye, g.eye, 16);
+  std::memcpy(p2m, g.p2m.e, 16 * sizeof(real));
+  std::memcpy(m2v, g.m2v.e, 16 * sizeof(real));
+  std::memcpy(mv, g.mv.e, 16 * sizeof(real));
+  std::memcpy(v2m, g.v2m.e, 16 * sizeof(real));
+  std::memcpy(eye, g.eye, 4 * sizeof(real));
 }
 
 // GenerateImage_MT (TypicalRayProducer.core.h:123-225).
-void orc_forward(const orc_scan *s, double angle_deg, const float *vol, float *img, float *len, float *weight) {
+void orc_forward(const orc_scan *s, double angle_deg, const real *vol, real *img, real *len, real *weight) {
   set_threads(s->threads);
   ProjGeom g = make_geometry(s, angle_deg);
   const int W = s->det[0], H = s->det[1];
-  const float sd = orc_sample_distance(s->vs);
+  const real sd = orc_sample_distance(s->vs);
   Vol v{vol, {s->vol[0], s->vol[1], s->vol[2]}};
 #pragma omp parallel for schedule(dynamic, 1)
   for (int j = 0; j < H; ++j)
     for (int i = 0; i < W; ++i) {
       int k = i + j * W;
-      float vz[4], vu[4], tn, tf;
-      produce_ray(g, s->vol, (float)i, (float)j, vz, vu, tn, tf);
-      float sumw = 0.0f;
+      real vz[4], vu[4], tn, tf;
+      produce_ray(g, s->vol, (real)i, (real)j, vz, vu, tn, tf);
+      real sumw = 0.0f;
       double value = 0.0f;
       len[k] = 0.0f;
       if (tn < tf) {
@@ -500,25 +503,25 @@ void orc_forward(const orc_scan *s, double angle_deg, const float *vol, float *i
         value = cast_ray(v, vz, vu, tn, tf, sd, sumw, nullptr);
       }
       weight[k] = sumw;
-      img[k] = (float)value;
+      img[k] = (real)value;
     }
 }
 
 // Back-projection mode of the same traversal, single-threaded (the
 // reference's += on shared voxels races under OpenMP).
-void orc_ray_backproject(const orc_scan *s, double angle_deg, const float *corr, float *contrib, float *weight) {
+void orc_ray_backproject(const orc_scan *s, double angle_deg, const real *corr, real *contrib, real *weight) {
   ProjGeom g = make_geometry(s, angle_deg);
   const int W = s->det[0], H = s->det[1];
-  const float sd = orc_sample_distance(s->vs);
+  const real sd = orc_sample_distance(s->vs);
   size_t nv = (size_t)s->vol[0] * s->vol[1] * s->vol[2];
-  std::memset(contrib, 0, nv * 4);
-  std::memset(weight, 0, nv * 4);
+  std::memset(contrib, 0, nv * sizeof(real));
+  std::memset(weight, 0, nv * sizeof(real));
   Vol v{nullptr, {s->vol[0], s->vol[1], s->vol[2]}};
   for (int j = 0; j < H; ++j)
     for (int i = 0; i < W; ++i) {
-      float vz[4], vu[4], tn, tf;
-      produce_ray(g, s->vol, (float)i, (float)j, vz, vu, tn, tf);
-      float sumw = 0.0f;
+      real vz[4], vu[4], tn, tf;
+      produce_ray(g, s->vol, (real)i, (real)j, vz, vu, tn, tf);
+      real sumw = 0.0f;
       if (tn < tf) {
         Splat sp{contrib, weight, corr[i + j * W]};
         cast_ray(v, vz, vu, tn, tf, sd, sumw, &sp);
@@ -527,47 +530,47 @@ void orc_ray_backproject(const orc_scan *s, double angle_deg, const float *corr,
 }
 
 // WaP_Tomo.cpp:1530-1555: c = (F p - F Ax - y)/(F len + 1), y += alpha c, F = 1.
-void orc_correction(int n, const float *p, const float *ax, const float *len, float *dual, double alpha, float *c) {
-  const float F = std::sqrt(2 * (1.0f / 2));
+void orc_correction(int n, const real *p, const real *ax, const real *len, real *dual, double alpha, real *c) {
+  const real F = std::sqrt(2 * (1.0f / 2));
   for (int k = 0; k < n; ++k) {
-    float y = dual ? dual[k] : 0.0f;
-    c[k] = (float)(F * p[k] - F * ax[k] - y) / (float)(F * len[k] + 1.0f);
+    real y = dual ? dual[k] : 0.0f;
+    c[k] = (real)(F * p[k] - F * ax[k] - y) / (real)(F * len[k] + 1.0f);
     if (dual) dual[k] += alpha * c[k];
   }
 }
 
-void orc_bp_voxel(const orc_scan *s, double angle_deg, const float *corr, const int box[6], int mode, float *vol) {
+void orc_bp_voxel(const orc_scan *s, double angle_deg, const real *corr, const int box[6], int mode, real *vol) {
   set_threads(s->threads);
   ProjGeom g = make_geometry(s, angle_deg);
   const int W = s->det[0], H = s->det[1];
   const int *d = s->vol;
   const double halfW = (W - 1) * s->ds * 0.5f, halfH = (H - 1) * s->ds * 0.5f;
-  const float sdd = (float)s->sdd;
+  const real sdd = (real)s->sdd;
   const double ds = s->ds;
   const double alpha = s->alpha;
-  const float gmax = s->gmax;
+  const real gmax = s->gmax;
   const int iminY = W;
 #pragma omp parallel for
   for (int z = box[4]; z < box[5]; ++z)
     for (int y = box[2]; y < box[3]; ++y)
       for (int x = box[0]; x < box[1]; ++x) {
         size_t pos = x + (size_t)d[0] * (y + (size_t)d[1] * z);
-        float vec[4] = {(float)x, (float)y, (float)z, 1.0f};
-        float det[4];
+        real vec[4] = {(real)x, (real)y, (real)z, 1.0f};
+        real det[4];
         m4_vec(g.mvv2m.e, vec, det);
-        float _px = halfW - (det[0] / det[2]) * sdd;
-        float _py = halfH - (det[1] / det[2]) * sdd;
+        real _px = halfW - (det[0] / det[2]) * sdd;
+        real _py = halfH - (det[1] / det[2]) * sdd;
         _px = _px / ds;
         _py = _py / ds;
         int px = (int)_px, py = (int)_py;
-        float dx = _px - px, dy = _py - py;
+        real dx = _px - px, dy = _py - py;
         if (px < 2 || px >= W - 2 || py < 2 || py >= H - 2) continue;
-        const float *pC = corr + py * W + px;
-        float pimg[4][4] = {{pC[-1 - iminY], pC[-1], pC[-1 + iminY], pC[-1 + 2 * iminY]},
+        const real *pC = corr + py * W + px;
+        real pimg[4][4] = {{pC[-1 - iminY], pC[-1], pC[-1 + iminY], pC[-1 + 2 * iminY]},
                             {pC[-iminY], pC[0], pC[iminY], pC[2 * iminY]},
                             {pC[1 - iminY], pC[1], pC[1 + iminY], pC[1 + 2 * iminY]},
                             {pC[2 - iminY], pC[2], pC[2 + iminY], pC[2 + 2 * iminY]}};
-        float gv = bicubic_interp(pimg, dx, dy);
+        real gv = bicubic_interp(pimg, dx, dy);
         if (mode == 0) {
           vol[pos] += alpha * gv;
           vol[pos] = mac_max(mac_min(gmax, vol[pos]), 0);
@@ -577,28 +580,28 @@ void orc_bp_voxel(const orc_scan *s, double angle_deg, const float *corr, const 
       }
 }
 
-void orc_advect(const int dims[3], const float aabb[6], const float *vel, const float *src, int nc, float dt,
-                float *out, int threads) {
+void orc_advect(const int dims[3], const real aabb[6], const real *vel, const real *src, int nc, real dt,
+                real *out, int threads) {
   set_threads(threads);
   const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
-  const float tdt = -dt;  // advect calls trace(..., -dt)
+  const real tdt = -dt;  // advect calls trace(..., -dt)
 #pragma omp parallel for schedule(dynamic, 1)
   for (int k = 0; k < dims[2]; ++k)
     for (int j = 0; j < dims[1]; ++j)
       for (int i = 0; i < dims[0]; ++i) {
         const int gi[3] = {i, j, k};
-        float p[3];
+        real p[3];
         for (int a = 0; a < 3; ++a) {
-          float gf = (float)gi[a];
-          p[a] = (float)(aabb[2 * a] + (gf + 0.5) * (aabb[2 * a + 1] - aabb[2 * a]) / (float)dims[a]);
+          real gf = (real)gi[a];
+          p[a] = (real)(aabb[2 * a] + (gf + 0.5) * (aabb[2 * a + 1] - aabb[2 * a]) / (real)dims[a]);
         }
         // trace (advection.h:101-115)
-        float v[3], p2[3], p0[3], q[3];
+        real v[3], p2[3], p0[3], q[3];
         sample_velocity(dims, aabb, vel, p, v);
         for (int a = 0; a < 3; ++a) p2[a] = p[a] + tdt * v[a];
         sample_velocity(dims, aabb, vel, p2, v);
         for (int a = 0; a < 3; ++a) p0[a] = p2[a] - tdt * v[a];
-        for (int a = 0; a < 3; ++a) q[a] = p2[a] + (float)(0.5 * (float)(p[a] - p0[a]));
+        for (int a = 0; a < 3; ++a) q[a] = p2[a] + (real)(0.5 * (real)(p[a] - p0[a]));
         for (int c = 0; c < nc; ++c) {
           Img I{src + c * nv, {dims[0], dims[1], dims[2]}};
           out[c * nv + i + (size_t)dims[0] * (j + (size_t)dims[1] * k)] = sample_image(dims, aabb, I, q);
@@ -608,16 +611,16 @@ void orc_advect(const int dims[3], const float aabb[6], const float *vel, const 
 
 // CImg::deriche order 0 with Neumann boundaries (CImg.h:32917-33010) applied
 // along x, then y, then z (CImg::blur, CImg.h:33249-33262).
-void orc_blur(const int dims[3], int nc, float sigma, const float *src, float *out) {
+void orc_blur(const int dims[3], int nc, real sigma, const real *src, real *out) {
   const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
-  std::memcpy(out, src, nv * nc * 4);
-  const float nsigma = sigma >= 0 ? sigma : 0.0f;
+  std::memcpy(out, src, nv * nc * sizeof(real));
+  const real nsigma = sigma >= 0 ? sigma : 0.0f;
   if (nsigma < 0.1f) return;
-  const float nnsigma = nsigma < 0.1f ? 0.1f : nsigma, alpha = 1.695f / nnsigma, ema = (float)std::exp(-alpha),
-              ema2 = (float)std::exp(-2 * alpha), b1 = -2 * ema, b2 = ema2;
-  const float k = (1 - ema) * (1 - ema) / (1 + 2 * alpha * ema - ema2);
-  const float a0 = k, a1 = k * (alpha - 1) * ema, a2 = k * (alpha + 1) * ema, a3 = -k * ema2;
-  const float coefp = (a0 + a1) / (1 + b1 + b2), coefn = (a2 + a3) / (1 + b1 + b2);
+  const real nnsigma = nsigma < 0.1f ? 0.1f : nsigma, alpha = 1.695f / nnsigma, ema = (real)std::exp(-alpha),
+              ema2 = (real)std::exp(-2 * alpha), b1 = -2 * ema, b2 = ema2;
+  const real k = (1 - ema) * (1 - ema) / (1 + 2 * alpha * ema - ema2);
+  const real a0 = k, a1 = k * (alpha - 1) * ema, a2 = k * (alpha + 1) * ema, a3 = -k * ema2;
+  const real coefp = (a0 + a1) / (1 + b1 + b2), coefn = (a2 + a3) / (1 + b1 + b2);
   const size_t stride[3] = {1, (size_t)dims[0], (size_t)dims[0] * dims[1]};
   for (int axis = 0; axis < 3; ++axis) {
     const int N = dims[axis];
@@ -628,22 +631,22 @@ void orc_blur(const int dims[3], int nc, float sigma, const float *src, float *o
     for (int c = 0; c < nc; ++c)
       for (int u = 0; u < dims[o2]; ++u)
         for (int w = 0; w < dims[o1]; ++w) {
-          float *ptr = out + c * nv + w * stride[o1] + u * stride[o2];
-          std::vector<float> Y(N);
-          float yb = 0, yp = 0, xp = 0;
+          real *ptr = out + c * nv + w * stride[o1] + u * stride[o2];
+          std::vector<real> Y(N);
+          real yb = 0, yp = 0, xp = 0;
           xp = ptr[0];
           yb = yp = coefp * xp;
           for (int m = 0; m < N; ++m) {
-            const float xc = ptr[m * off];
-            const float yc = Y[m] = a0 * xc + a1 * xp - b1 * yp - b2 * yb;
+            const real xc = ptr[m * off];
+            const real yc = Y[m] = a0 * xc + a1 * xp - b1 * yp - b2 * yb;
             xp = xc;
             yb = yp;
             yp = yc;
           }
-          float xn = ptr[(N - 1) * off], xa = xn, yn = coefn * xn, ya = yn;
+          real xn = ptr[(N - 1) * off], xa = xn, yn = coefn * xn, ya = yn;
           for (int n = N - 1; n >= 0; --n) {
-            const float xc = ptr[n * off];
-            const float yc = a2 * xn + a3 * xa - b1 * yn - b2 * ya;
+            const real xc = ptr[n * off];
+            const real yc = a2 * xn + a3 * xa - b1 * yn - b2 * ya;
             xa = xn;
             xn = xc;
             ya = yn;
@@ -657,8 +660,8 @@ void orc_blur(const int dims[3], int nc, float sigma, const float *src, float *o
 // CImg::get_resize(sx,sy,sz,sc, 5, 0): per axis, moving average when
 // shrinking (CImg.h:28135-28213) or the double-precision cubic when growing
 // (CImg.h:28432-28610), axes in the order x, y, z.
-void orc_resize(const int dims[3], int nc, const float *src, const int odims[3], float *out) {
-  std::vector<float> cur(src, src + (size_t)dims[0] * dims[1] * dims[2] * nc);
+void orc_resize(const int dims[3], int nc, const real *src, const int odims[3], real *out) {
+  std::vector<real> cur(src, src + (size_t)dims[0] * dims[1] * dims[2] * nc);
   int cd[3] = {dims[0], dims[1], dims[2]};
   for (int axis = 0; axis < 3; ++axis) {
     const int Sin = cd[axis], Sout = odims[axis];
@@ -668,7 +671,7 @@ void orc_resize(const int dims[3], int nc, const float *src, const int odims[3],
     const size_t in_stride[3] = {1, (size_t)cd[0], (size_t)cd[0] * cd[1]};
     const size_t out_stride[3] = {1, (size_t)nd[0], (size_t)nd[0] * nd[1]};
     const size_t in_nv = (size_t)cd[0] * cd[1] * cd[2], out_nv = (size_t)nd[0] * nd[1] * nd[2];
-    std::vector<float> nxt(out_nv * nc, 0.0f);
+    std::vector<real> nxt(out_nv * nc, 0.0f);
     const int o1 = (axis + 1) % 3, o2 = (axis + 2) % 3;
     if (Sin == 1) {
       // nearest-neighbour replication (CImg falls back to interpolation 1)
@@ -700,11 +703,11 @@ void orc_resize(const int dims[3], int nc, const float *src, const int odims[3],
         for (int u = 0; u < cd[o2]; ++u)
           for (int w = 0; w < cd[o1]; ++w)
             for (int t = 0; t < Sout; ++t) {
-              float acc = 0.0f;
+              real acc = 0.0f;
               for (auto &tp : taps[t])
                 acc += cur[ch * in_nv + w * in_stride[o1] + u * in_stride[o2] + tp.first * in_stride[axis]] *
-                       (float)tp.second;
-              acc /= (float)(unsigned)Sin;
+                       (real)tp.second;
+              acc /= (real)(unsigned)Sin;
               nxt[ch * out_nv + w * out_stride[o1] + u * out_stride[o2] + t * out_stride[axis]] = acc;
             }
     } else {
@@ -724,7 +727,7 @@ void orc_resize(const int dims[3], int nc, const float *src, const int odims[3],
       for (int ch = 0; ch < nc; ++ch)
         for (int u = 0; u < cd[o2]; ++u)
           for (int w = 0; w < cd[o1]; ++w) {
-            const float *line = cur.data() + ch * in_nv + w * in_stride[o1] + u * in_stride[o2];
+            const real *line = cur.data() + ch * in_nv + w * in_stride[o1] + u * in_stride[o2];
             const size_t st = in_stride[axis];
             for (int x = 0; x < Sout; ++x) {
               const int i = (int)base[x];
@@ -736,17 +739,17 @@ void orc_resize(const int dims[3], int nc, const float *src, const int odims[3],
               const double val = val1 + 0.5f * (t * (-val0 + val2) + t * t * (2 * val0 - 5 * val1 + 4 * val2 - val3) +
                                                 t * t * t * (-val0 + 3 * val1 - 3 * val2 + val3));
               nxt[ch * out_nv + w * out_stride[o1] + u * out_stride[o2] + x * out_stride[axis]] =
-                  (float)(val < vmin ? vmin : val > vmax ? vmax : val);
+                  (real)(val < vmin ? vmin : val > vmax ? vmax : val);
             }
           }
     }
     cur.swap(nxt);
     cd[axis] = Sout;
   }
-  std::memcpy(out, cur.data(), cur.size() * 4);
+  std::memcpy(out, cur.data(), cur.size() * sizeof(real));
 }
 
-void orc_gradient(const int dims[3], const float *src, float *gx, float *gy, float *gz) {
+void orc_gradient(const int dims[3], const real *src, real *gx, real *gy, real *gz) {
   Img I{src, {dims[0], dims[1], dims[2]}};
   for (int z = 0; z < dims[2]; ++z)
     for (int y = 0; y < dims[1]; ++y)
@@ -771,31 +774,31 @@ struct Grid {
   size_t id(int i, int j, int k) const { return i + (size_t)n[0] * (j + (size_t)n[1] * k); }
 };
 
-inline float dxp3(const float *d, const Grid &g, int i, int j, int k) {
+inline real dxp3(const real *d, const Grid &g, int i, int j, int k) {
   return i < g.n[0] - 1 ? d[g.id(i + 1, j, k)] - d[g.id(i, j, k)] : 0.0f;
 }
-inline float dyp3(const float *d, const Grid &g, int i, int j, int k) {
+inline real dyp3(const real *d, const Grid &g, int i, int j, int k) {
   return j < g.n[1] - 1 ? d[g.id(i, j + 1, k)] - d[g.id(i, j, k)] : 0.0f;
 }
-inline float dzp3(const float *d, const Grid &g, int i, int j, int k) {
+inline real dzp3(const real *d, const Grid &g, int i, int j, int k) {
   return k < g.n[2] - 1 ? d[g.id(i, j, k + 1)] - d[g.id(i, j, k)] : 0.0f;
 }
-inline float dxm3(const float *d, const Grid &g, int i, int j, int k) {
+inline real dxm3(const real *d, const Grid &g, int i, int j, int k) {
   if (i > 0 && i < g.n[0] - 1) return d[g.id(i, j, k)] - d[g.id(i - 1, j, k)];
   if (i == 0) return d[g.id(i, j, k)];
   return -d[g.id(i - 1, j, k)];
 }
-inline float dym3(const float *d, const Grid &g, int i, int j, int k) {
+inline real dym3(const real *d, const Grid &g, int i, int j, int k) {
   if (j > 0 && j < g.n[1] - 1) return d[g.id(i, j, k)] - d[g.id(i, j - 1, k)];
   if (j == 0) return d[g.id(i, j, k)];
   return -d[g.id(i, j - 1, k)];
 }
-inline float dzm3(const float *d, const Grid &g, int i, int j, int k) {
+inline real dzm3(const real *d, const Grid &g, int i, int j, int k) {
   if (k > 0 && k < g.n[2] - 1) return d[g.id(i, j, k)] - d[g.id(i, j, k - 1)];
   if (k == 0) return d[g.id(i, j, k)];
   return -d[g.id(i, j, k - 1)];
 }
-inline float my_abs(float x) { return x > 0 ? x : -x; }
+inline real my_abs(real x) { return x > 0 ? x : -x; }
 
 }  // namespace
 
@@ -805,14 +808,14 @@ extern "C" {
 
 double orc_last_pd_seconds() { return g_last_pd_seconds; }
 
-int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V, float *Y1, float *Y2, float *Y3,
-                   float *Y4, float tol, float lambda, int max_iters, int nwarps, const float aabb[6],
+int orc_flow_level(const int dims[3], const real *I1, const real *I2, real *V, real *Y1, real *Y2, real *Y3,
+                   real *Y4, real tol, real lambda, int max_iters, int nwarps, const real aabb[6],
                    const int roi6[6], int deterministic, int *iters_out) {
   const Grid g{{dims[0], dims[1], dims[2]}};
   const int nPx = dims[0] * dims[1] * dims[2];
   const size_t n = (size_t)nPx;
-  std::vector<float> v[3], vOld[3], y[9], yOld[9], Kty[3], KtyOld[3], Kx[9], KxOld[9];
-  std::vector<float> y4(n), y4Old(n), Kx4(n, 0.0f), Kx4Old(n, 0.0f), ux(n, 0.0f), uy(n, 0.0f), uz(n, 0.0f),
+  std::vector<real> v[3], vOld[3], y[9], yOld[9], Kty[3], KtyOld[3], Kx[9], KxOld[9];
+  std::vector<real> y4(n), y4Old(n), Kx4(n, 0.0f), Kx4Old(n, 0.0f), ux(n, 0.0f), uy(n, 0.0f), uz(n, 0.0f),
       ut(n, 0.0f), tau[3], sigma2(n);
   for (int c = 0; c < 3; ++c) {
     v[c].assign(V + c * n, V + (c + 1) * n);
@@ -821,7 +824,7 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
     KtyOld[c].assign(n, 0.0f);
     tau[c].assign(n, 0.0f);
   }
-  const float *Ys[3] = {Y1, Y2, Y3};
+  const real *Ys[3] = {Y1, Y2, Y3};
   for (int a = 0; a < 3; ++a)
     for (int c = 0; c < 3; ++c) {
       y[3 * a + c].assign(Ys[a] + c * n, Ys[a] + (c + 1) * n);
@@ -830,16 +833,16 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
       KxOld[3 * a + c].assign(n, 0.0f);
     }
   y4.assign(Y4, Y4 + n);
-  const float sigma1 = std::min(1.0f / 3.0f, std::min(1.0f / 3.0f, 1.0f / 3.0f));
+  const real sigma1 = std::min(1.0f / 3.0f, std::min(1.0f / 3.0f, 1.0f / 3.0f));
   const int *roi = roi6;
   const int x0 = roi[0], x1 = dims[0] - roi[1], y0 = roi[2], y1 = dims[1] - roi[3], z0 = roi[4], z1 = dims[2] - roi[5];
-  float p = 0.0f, d = 0.0f;
+  real p = 0.0f, d = 0.0f;
   int total = 0;
   double pd_seconds = 0.0;
-  std::vector<float> Vimg(3 * n), warp(n), gx(n), gy(n), gz(n);
+  std::vector<real> Vimg(3 * n), warp(n), gx(n), gy(n), gz(n);
   for (int w = 0; w < nwarps; ++w) {
     // _inputV holds v inside the ROI (written by the primal) and the input outside.
-    for (int c = 0; c < 3; ++c) std::memcpy(Vimg.data() + c * n, V + c * n, n * 4);
+    for (int c = 0; c < 3; ++c) std::memcpy(Vimg.data() + c * n, V + c * n, n * sizeof(real));
     orc_advect(dims, aabb, Vimg.data(), I2, 1, -1.0f, warp.data(), 0);
     orc_gradient(dims, warp.data(), gx.data(), gy.data(), gz.data());
 #pragma omp parallel for
@@ -864,8 +867,8 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
       sigma2[i] = 1.0f / sigma2[i];
     }
     int it = 0;
-    float err = 1.0f;
-    const float *uu[3] = {ux.data(), uy.data(), uz.data()};
+    real err = 1.0f;
+    const real *uu[3] = {ux.data(), uy.data(), uz.data()};
     const double t_pd = omp_get_wtime();
     while (err > tol && it <= max_iters) {
       ++it;
@@ -875,7 +878,7 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
         d = 0.0f;
       }
       // primal (optical_flow.h:489-553)
-      auto primal = [&](int i, int j, int k, float &acc) {
+      auto primal = [&](int i, int j, int k, real &acc) {
         size_t t = g.id(i, j, k);
         if (res)
           for (int c = 0; c < 3; ++c) {
@@ -900,7 +903,7 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
           for (int j = y0; j < y1; ++j)
             for (int i = x0; i < x1; ++i) primal(i, j, k, p);
       } else {
-        float pp = 0.0f;
+        real pp = 0.0f;
 #pragma omp parallel for reduction(+ : pp)
         for (int k = z0; k < z1; ++k)
           for (int j = y0; j < y1; ++j)
@@ -908,7 +911,7 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
         p += pp;
       }
       // dual (optical_flow.h:567-813), norm != 4 branch
-      auto dual = [&](int t, float &acc) {
+      auto dual = [&](int t, real &acc) {
         int i = t % dims[0], j = (t / dims[0]) % dims[1], k = t / (dims[0] * dims[1]);
         if (res) {
           for (int q = 0; q < 9; ++q) yOld[q][t] = y[q][t];
@@ -923,14 +926,14 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
         }
         Kx4[t] = ux[t] * v[0][t] + uy[t] * v[1][t] + uz[t] * v[2][t];
         for (int q = 0; q < 9; ++q) {
-          float yt = y[q][t] + sigma1 * (Kx[q][t] + Kx[q][t] - KxOld[q][t]);
+          real yt = y[q][t] + sigma1 * (Kx[q][t] + Kx[q][t] - KxOld[q][t]);
           y[q][t] = yt * lambda / (lambda + 2 * sigma1);
         }
         y4[t] = std_max(-1.0f, std_min(1.0f, y4[t] + sigma2[t] * (Kx4[t] + Kx4[t] - Kx4Old[t] + ut[t])));
         if (res) {
-          float s = 0.0f;
+          real s = 0.0f;
           for (int q = 0; q < 9; ++q) {
-            float term = std::abs((yOld[q][t] - y[q][t]) / sigma1 - KxOld[q][t] + Kx[q][t]);
+            real term = std::abs((yOld[q][t] - y[q][t]) / sigma1 - KxOld[q][t] + Kx[q][t]);
             s = (q == 0) ? term : s + term;
           }
           s = s + std::abs((y4Old[t] - y4[t]) / sigma2[t] - Kx4Old[t] + Kx4[t]);
@@ -940,12 +943,12 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
       if (deterministic) {
         for (int t = 0; t < nPx; ++t) dual(t, d);
       } else {
-        float dd = 0.0f;
+        real dd = 0.0f;
 #pragma omp parallel for reduction(+ : dd)
         for (int t = 0; t < nPx; ++t) dual(t, dd);
         d += dd;
       }
-      if (res) err = (d * d + p * p) / (float)nPx;
+      if (res) err = (d * d + p * p) / (real)nPx;
     }
     pd_seconds += omp_get_wtime() - t_pd;
     if (iters_out) iters_out[w] = it;
@@ -968,19 +971,19 @@ int orc_flow_level(const int dims[3], const float *I1, const float *I2, float *V
   return total;
 }
 
-int orc_flow_multiscale(const int dims[3], const float *I1, const float *I2, const float *V0, float tol,
-                        float lambda, int max_iters, int nwarps, float eta, float sigma, int scales,
-                        const int cut6[6], int deterministic, float *Vout) {
+int orc_flow_multiscale(const int dims[3], const real *I1, const real *I2, const real *V0, real tol,
+                        real lambda, int max_iters, int nwarps, real eta, real sigma, int scales,
+                        const int cut6[6], int deterministic, real *Vout) {
   const size_t n = (size_t)dims[0] * dims[1] * dims[2];
-  std::vector<float> b1(n), b2(n);
+  std::vector<real> b1(n), b2(n);
   orc_blur(dims, 1, sigma, I1, b1.data());
   orc_blur(dims, 1, sigma, I2, b2.data());
   struct Lvl {
     int d[3];
-    std::vector<float> i1, i2, v, y1, y2, y3, y4;
+    std::vector<real> i1, i2, v, y1, y2, y3, y4;
   };
   std::vector<Lvl> L(scales);
-  float t_eta = 1.0f;
+  real t_eta = 1.0f;
   for (int s = 0; s < scales; ++s) {
     Lvl &l = L[scales - 1 - s];  // reversed: coarse first
     l.d[0] = (int)(dims[0] * t_eta);
@@ -1000,13 +1003,13 @@ int orc_flow_multiscale(const int dims[3], const float *I1, const float *I2, con
     t_eta = t_eta * eta;
   }
   int total = 0;
-  const float aabb[6] = {0, (float)dims[0], 0, (float)dims[1], 0, (float)dims[2]};
+  const real aabb[6] = {0, (real)dims[0], 0, (real)dims[1], 0, (real)dims[2]};
   for (int s = 0; s < scales; ++s) {
     Lvl &l = L[s];
     int roi[6];
     for (int i = 0; i < 6; ++i) {
       int a = i / 2;
-      roi[i] = (float)cut6[i] * ((float)l.d[a] / (float)dims[a]);
+      roi[i] = (real)cut6[i] * ((real)l.d[a] / (real)dims[a]);
     }
     total += orc_flow_level(l.d, l.i1.data(), l.i2.data(), l.v.data(), l.y1.data(), l.y2.data(), l.y3.data(),
                             l.y4.data(), tol, lambda, max_iters, nwarps, aabb, roi, deterministic, nullptr);
@@ -1019,18 +1022,18 @@ int orc_flow_multiscale(const int dims[3], const float *I1, const float *I2, con
       orc_resize(l.d, 1, l.y4.data(), nx.d, nx.y4.data());
     }
   }
-  std::memcpy(Vout, L[scales - 1].v.data(), 3 * n * 4);
+  std::memcpy(Vout, L[scales - 1].v.data(), 3 * n * sizeof(real));
   return total;
 }
 
 // SART_Proximal_Operator (WaP_Tomo.cpp:1424-1678).
-void orc_sart_prox(const orc_scan *s, const double *angles, const float *projs, int pstart, int pend, int nb_sart,
-                   const int box[6], float *vol, float *dual_rows) {
+void orc_sart_prox(const orc_scan *s, const double *angles, const real *projs, int pstart, int pend, int nb_sart,
+                   const int box[6], real *vol, real *dual_rows) {
   const int W = s->det[0], H = s->det[1];
   const size_t np = (size_t)W * H;
   const size_t nv = (size_t)s->vol[0] * s->vol[1] * s->vol[2];
-  std::memset(dual_rows, 0, sizeof(float) * np * s->nproj);
-  std::vector<float> img(np), len(np), wt(np), c(np);
+  std::memset(dual_rows, 0, sizeof(real) * np * s->nproj);
+  std::vector<real> img(np), len(np), wt(np), c(np);
   const int num = pend - pstart + 1;
   std::vector<int> order(num);
   for (int i = 0; i < num; ++i) order[i] = (i % 2 == 0) ? pstart + i / 2 : pend - i / 2;
@@ -1045,14 +1048,14 @@ void orc_sart_prox(const orc_scan *s, const double *angles, const float *projs, 
 }
 
 // WarpAndProjct (WaP_Tomo.cpp:1207-1421) with imROI == 1.
-void orc_warp_and_project(const orc_scan *s, const double *angles, const float *projs, int proj, float rtime,
-                          const float *flow_fwd, const float *flow_adj, float *vol) {
+void orc_warp_and_project(const orc_scan *s, const double *angles, const real *projs, int proj, real rtime,
+                          const real *flow_fwd, const real *flow_adj, real *vol) {
   const int W = s->det[0], H = s->det[1];
   const size_t np = (size_t)W * H;
   const int *d = s->vol;
   const size_t nv = (size_t)d[0] * d[1] * d[2];
-  const float aabb[6] = {0, (float)d[0], 0, (float)d[1], 0, (float)d[2]};
-  std::vector<float> warped(nv), img(np), len(np), wt(np), c(np), delta(nv, 0.0f), back(nv);
+  const real aabb[6] = {0, (real)d[0], 0, (real)d[1], 0, (real)d[2]};
+  std::vector<real> warped(nv), img(np), len(np), wt(np), c(np), delta(nv, 0.0f), back(nv);
   orc_advect(d, aabb, flow_fwd, vol, 1, rtime, warped.data(), s->threads);
   orc_forward(s, angles[proj], warped.data(), img.data(), len.data(), wt.data());
   orc_correction((int)np, projs + np * proj, img.data(), len.data(), nullptr, s->alpha, c.data());
@@ -1060,22 +1063,22 @@ void orc_warp_and_project(const orc_scan *s, const double *angles, const float *
   orc_bp_voxel(s, angles[proj], c.data(), full, 1, delta.data());
   orc_advect(d, aabb, flow_adj, delta.data(), 1, -rtime, back.data(), s->threads);
   const double alpha = s->alpha;
-  const float gmax = s->gmax;
+  const real gmax = s->gmax;
   for (size_t i = 0; i < nv; ++i) {
-    float x = (float)((double)vol[i] + (double)back[i] * alpha);
+    real x = (real)((double)vol[i] + (double)back[i] * alpha);
     x = (x < 0.0f) ? 0.0f : ((x > gmax) ? gmax : x);  // CImg::cut(0, G_Max)
     vol[i] = mac_max(x * 1.0f, 0.0f);
   }
 }
 
 // CP dual for frame f (WaP_Tomo.cpp:586-619).
-void orc_cp_dual(const orc_scan *s, const int box[6], const float *xbar_f, const float *xbar_next, float *ytv_f,
-                 float *ytp_f) {
+void orc_cp_dual(const orc_scan *s, const int box[6], const real *xbar_f, const real *xbar_next, real *ytv_f,
+                 real *ytp_f) {
   const int *d = s->vol;
   const size_t nv = (size_t)d[0] * d[1] * d[2];
-  const float L = 8.0f, tau = 1.0f;
-  const float sigma = .9 / (L * tau);
-  const float tv_w = (float)s->tv_w, tp_w = (float)s->tp_w, huber = 1.0f;
+  const real L = 8.0f, tau = 1.0f;
+  const real sigma = .9 / (L * tau);
+  const real tv_w = (real)s->tv_w, tp_w = (real)s->tp_w, huber = 1.0f;
   for (size_t i = 0; i < nv; ++i) ytp_f[i] += sigma * (xbar_next[i] - xbar_f[i]);
   const Grid g{{d[0], d[1], d[2]}};
   for (int k = box[4]; k < box[5]; ++k)
@@ -1091,24 +1094,24 @@ void orc_cp_dual(const orc_scan *s, const int box[6], const float *xbar_f, const
 }
 
 // CP primal for frame f before its SART call (WaP_Tomo.cpp:622-660).
-void orc_cp_primal(const orc_scan *s, const int box[6], int frame, const float *ytp_prev, const float *ytp_f,
-                   const float *ytv_f, float *vol, float *xprev) {
+void orc_cp_primal(const orc_scan *s, const int box[6], int frame, const real *ytp_prev, const real *ytp_f,
+                   const real *ytv_f, real *vol, real *xprev) {
   const int *d = s->vol;
   const size_t nv = (size_t)d[0] * d[1] * d[2];
-  const float tau = 1.0f;
-  std::memcpy(xprev, vol, nv * 4);
+  const real tau = 1.0f;
+  std::memcpy(xprev, vol, nv * sizeof(real));
   if (frame == 0) {
     for (size_t i = 0; i < nv; ++i) vol[i] -= tau * (0.0f - ytp_f[i]);
   } else {
     for (size_t i = 0; i < nv; ++i) vol[i] -= tau * (ytp_prev[i] - ytp_f[i]);
   }
   const Grid g{{d[0], d[1], d[2]}};
-  const float gmax = s->gmax;
+  const real gmax = s->gmax;
   for (int k = box[4]; k < box[5]; ++k)
     for (int j = box[2]; j < box[3]; ++j)
       for (int i = box[0]; i < box[1]; ++i) {
         size_t t = g.id(i, j, k);
-        float y1 = -(ytv_f[t] - ytv_f[g.id(i - 1, j, k)] + ytv_f[nv + t] - ytv_f[nv + g.id(i, j - 1, k)] +
+        real y1 = -(ytv_f[t] - ytv_f[g.id(i - 1, j, k)] + ytv_f[nv + t] - ytv_f[nv + g.id(i, j - 1, k)] +
                      ytv_f[2 * nv + t] - ytv_f[2 * nv + g.id(i, j, k - 1)]);
         vol[t] -= (tau * y1);
         vol[t] = mac_max(mac_min(gmax, vol[t]), 0);
@@ -1116,7 +1119,7 @@ void orc_cp_primal(const orc_scan *s, const int box[6], int frame, const float *
 }
 
 // X_bar = 2 x - x_prev over the ROI (WaP_Tomo.cpp:675-689).
-void orc_cp_overrelax(const int dims[3], const int box[6], const float *vol, const float *xprev, float *xbar) {
+void orc_cp_overrelax(const int dims[3], const int box[6], const real *vol, const real *xprev, real *xbar) {
   const Grid g{{dims[0], dims[1], dims[2]}};
   for (int k = box[4]; k < box[5]; ++k)
     for (int j = box[2]; j < box[3]; ++j)
@@ -1126,24 +1129,24 @@ void orc_cp_overrelax(const int dims[3], const int box[6], const float *vol, con
       }
 }
 
-int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double *angles, const float *projs,
-                        int level, float *vols, float *flows, float *ytv, float *ytp, float *xbar, float *xprev,
+int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double *angles, const real *projs,
+                        int level, real *vols, real *flows, real *ytv, real *ytp, real *xbar, real *xprev,
                         int *flow_iters_total) {
   const int *d = s->vol;
   const size_t nv = (size_t)d[0] * d[1] * d[2];
   std::vector<int> st(130), en(130);
-  std::vector<float> ft(130);
-  float tunit;
+  std::vector<real> ft(130);
+  real tunit;
   const int F = orc_level_frames(s->nframes_cli, s->nproj, level, st.data(), en.data(), ft.data(), &tunit);
   // m_roi = cut * dims / level-0 dims (WaP_Tomo.cpp:529-536), level-0 dims == dims.
-  const int r = (int)((float)sch->cut * ((float)d[0] / (float)d[0]));
+  const int r = (int)((real)sch->cut * ((real)d[0] / (real)d[0]));
   const int box[6] = {r, d[0] - r, r, d[1] - r, r, d[2] - r};
   const size_t np = (size_t)s->det[0] * s->det[1];
-  std::vector<float> dual((size_t)s->nproj * np);
-  std::vector<float> zero(nv, 0.0f);
+  std::vector<real> dual((size_t)s->nproj * np);
+  std::vector<real> zero(nv, 0.0f);
   for (int icp = 1; icp <= sch->n_cp; ++icp)
     for (int f = 0; f < F; ++f) {
-      const float *xb_next = (f + 1 < F) ? xbar + (f + 1) * nv : zero.data();
+      const real *xb_next = (f + 1 < F) ? xbar + (f + 1) * nv : zero.data();
       orc_cp_dual(s, box, xbar + f * nv, xb_next, ytv + f * 3 * nv, ytp + f * nv);
       orc_cp_primal(s, box, f, f > 0 ? ytp + (f - 1) * nv : nullptr, ytp + f * nv, ytv + f * 3 * nv, vols + f * nv,
                     xprev + f * nv);
@@ -1153,59 +1156,59 @@ int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double
   int total = 0;
   const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
   for (int f = 0; f + 1 < F; ++f) {
-    std::vector<float> out(3 * nv);
+    std::vector<real> out(3 * nv);
     total += orc_flow_multiscale(d, vols + f * nv, vols + (f + 1) * nv, flows + f * 3 * nv, sch->flow_tol,
                                  sch->flow_lambda, sch->flow_iters, sch->flow_warps, sch->flow_eta, sch->flow_sigma,
                                  sch->flow_scales, cut6, sch->deterministic, out.data());
-    std::memcpy(flows + f * 3 * nv, out.data(), 3 * nv * 4);
+    std::memcpy(flows + f * 3 * nv, out.data(), 3 * nv * sizeof(real));
   }
   for (int wp = 0; wp < sch->nb_projwarp; ++wp)
     for (int f = 0; f < sch->wp_frames && f < F; ++f)
       for (int ik = st[f]; ik <= en[f]; ++ik) {
-        float td = (ik - ft[f]) / tunit;
+        real td = (ik - ft[f]) / tunit;
         td = mac_min(mac_max(-1.0f, td), 1.0f);
-        const float *ffwd = flows + (size_t)(td < 0.0f ? std::max(0, f - 1) : f) * 3 * nv;
-        const float *fadj = flows + (size_t)std::max(0, f - 1) * 3 * nv;
+        const real *ffwd = flows + (size_t)(td < 0.0f ? std::max(0, f - 1) : f) * 3 * nv;
+        const real *fadj = flows + (size_t)std::max(0, f - 1) * 3 * nv;
         orc_warp_and_project(s, angles, projs, ik, td, ffwd, fadj, vols + f * nv);
       }
   if (flow_iters_total) *flow_iters_total = total;
   return F;
 }
 
-// image_cg::cg<float> (cg.h:11-55) with image_blas dot/add (image_blas.h:9-91).
-int orc_cg_screened_laplacian(const int dims[3], float a, float b, const float *rhs, float *x, float rel_tol,
-                              int max_iters, float abs_tol, int mode) {
+// image_cg::cg<real> (cg.h:11-55) with image_blas dot/add (image_blas.h:9-91).
+int orc_cg_screened_laplacian(const int dims[3], real a, real b, const real *rhs, real *x, real rel_tol,
+                              int max_iters, real abs_tol, int mode) {
   const int W = dims[0], H = dims[1], D = dims[2];
   const size_t n = (size_t)W * H * D;
   auto id = [&](int i, int j, int k) { return i + (size_t)W * (j + (size_t)H * k); };
-  auto apply = [&](const std::vector<float> &in, std::vector<float> &out) {
+  auto apply = [&](const std::vector<real> &in, std::vector<real> &out) {
     for (int k = 0; k < D; ++k)
       for (int j = 0; j < H; ++j)
         for (int i = 0; i < W; ++i) {
-          float xc = in[id(i, j, k)];
-          float sn = in[id(i > 0 ? i - 1 : i, j, k)] + in[id(i < W - 1 ? i + 1 : i, j, k)] +
+          real xc = in[id(i, j, k)];
+          real sn = in[id(i > 0 ? i - 1 : i, j, k)] + in[id(i < W - 1 ? i + 1 : i, j, k)] +
                      in[id(i, j > 0 ? j - 1 : j, k)] + in[id(i, j < H - 1 ? j + 1 : j, k)] +
                      in[id(i, j, k > 0 ? k - 1 : k)] + in[id(i, j, k < D - 1 ? k + 1 : k)];
           out[id(i, j, k)] = a * xc - b * (sn - 6.0f * xc);
         }
   };
   // image_blas::dot iterates x outermost, then y, then z.
-  auto dot = [&](const std::vector<float> &u, const std::vector<float> &v) {
-    float res = 0.0f;
+  auto dot = [&](const std::vector<real> &u, const std::vector<real> &v) {
+    real res = 0.0f;
     for (int i = 0; i < W; ++i)
       for (int j = 0; j < H; ++j)
         for (int k = 0; k < D; ++k) res += u[id(i, j, k)] * v[id(i, j, k)];
     return res;
   };
-  std::vector<float> X(x, x + n), Ap(n), p(n), r(n);
+  std::vector<real> X(x, x + n), Ap(n), p(n), r(n);
   apply(X, Ap);
-  for (size_t i = 0; i < n; ++i) r[i] = (float)((double)rhs[i] + (double)Ap[i] * -1.0);
+  for (size_t i = 0; i < n; ++i) r[i] = (real)((double)rhs[i] + (double)Ap[i] * -1.0);
   p = r;
-  float rr, rr_old, rr_init, alpha;
+  real rr, rr_old, rr_init, alpha;
   rr = rr_old = rr_init = dot(r, r);
   int iters = 0;
   if (std::sqrt(rr) < abs_tol) {
-    std::memcpy(x, X.data(), n * 4);
+    std::memcpy(x, X.data(), n * sizeof(real));
     return 0;
   }
   for (int iter = 0; iter < max_iters; ++iter) {
@@ -1216,14 +1219,14 @@ int orc_cg_screened_laplacian(const int dims[3], float a, float b, const float *
     for (size_t i = 0; i < n; ++i) r[i] += Ap[i] * -alpha;
     rr = dot(r, r);
     if (std::sqrt(rr / rr_init) < rel_tol) break;
-    const float beta = rr / rr_old;
+    const real beta = rr / rr_old;
     if (mode == 1)
       for (size_t i = 0; i < n; ++i) p[i] = r[i] + 0.0f * beta;
     else
       for (size_t i = 0; i < n; ++i) p[i] = r[i] + p[i] * beta;
     rr_old = rr;
   }
-  std::memcpy(x, X.data(), n * 4);
+  std::memcpy(x, X.data(), n * sizeof(real));
   return iters;
 }
 

@@ -348,11 +348,12 @@ def test_cg_screened_laplacian(setup, orc, mode):
 
 
 def test_precision_form_fp16_flow_state(setup, orc, wapmod):
-    """The precision form (flow solver state in FP16; FP32 arithmetic with
-    fused multiply-adds and hardware reciprocals in the primal-dual iteration):
-    same iteration counts at a fixed count, the flow within 2e-2 relative L2
-    of the exact FP32 path, and an outer iteration's volumes within 1e-3
-    relative L2 of the oracle."""
+    """The precision form (flow solver state as FP16 pairs; FP32 arithmetic
+    with fused multiply-adds and hardware reciprocals in the primal-dual
+    iteration, float pyramid growth, fused-multiply-add warps): same iteration
+    counts at a fixed count, the flow within 2e-2 relative L2 of the exact FP32
+    path, and an outer iteration's volumes within 1e-3 relative L2 of the FP32
+    oracle and of the FP64 oracle."""
     s = setup
     torch, ctx = s["torch"], s["ctx"]
     aabb, I1, I2 = _flow_inputs(s, orc)
@@ -380,7 +381,13 @@ def test_precision_form_fp16_flow_state(setup, orc, wapmod):
                      ytv=np.zeros((F, 3, N, N, N), np.float32), ytp=np.zeros((F, N, N, N), np.float32),
                      xbar=np.zeros((F, N, N, N), np.float32), xprev=np.zeros((F, N, N, N), np.float32))
         orc.outer_iteration(s["oscan"], sched_o, s["ang"], s["projs"], 0, state)
+        # and against the FP64 oracle (the same algorithm in double)
+        o64 = O.Oracle(fp64=True)
+        state64 = {k: v.astype(np.float64) * 0 for k, v in state.items()}
+        o64.outer_iteration(s["oscan"], sched_o, s["ang"], o64.arr(s["projs"]), 0, state64)
         for f in range(F):
-            assert rel_l2(ctx.download_volume(f), state["vols"][f]) < 1e-3
+            got = ctx.download_volume(f)
+            assert rel_l2(got, state["vols"][f]) < 1e-3
+            assert rel_l2(got, state64["vols"][f]) < 1e-3
     finally:
         ctx.set_tuning("flow_bits", 32)
