@@ -159,7 +159,9 @@ WAP_API int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user);
  * changes).  key "pd_form": 0 = autotuned per grid size (default), 1 = the
  * fused primal-dual kernel, 2 = the primal + dual kernel pair, 3 = the
  * TMA-fed fused kernel (grids with nx % 4 == 0, else 2); "pd_zchunk": z
- * planes per block, 0 = autotuned / default.  One key changes results: the
+ * planes per block, 0 = autotuned / default; "fp_bricks": 1 (default) = the
+ * forward projector reads a 4x4x4 brick-layout copy of each volume, 0 = the
+ * linear volume.  One key changes results: the
  * precision form, "flow_bits" = 16 stores the flow solver's dual, flow and
  * linearisation as FP16 pairs during the primal-dual iterations and computes
  * them with fused multiply-adds and hardware reciprocals (FP64 residual sums;

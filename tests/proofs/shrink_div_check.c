@@ -14,14 +14,18 @@
 #include <stdlib.h>
 static float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
 static uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
-static float shrink_fast(float a, float den, float rinv, int *bad) {
+/* noinline: each candidate is evaluated as the scalar sequence written here;
+ * inlined into the OpenMP loop, GCC on aarch64 vectorised the loop and one
+ * input (a = -0) then came out as +0, while the same sequence compiled on its
+ * own gives -0 there as on x86 and on the GPU. */
+__attribute__((noinline)) static float shrink_fast(float a, float den, float rinv, int *bad) {
   const float q0 = a * rinv;
   const float en = fmaf(q0, den, -a);
   const float q = fmaf(-en, rinv, q0);
   *bad |= (a != 0.0f && fabsf(a) < 1.0e-30f) || !(fabsf(q0) < 3.0e38f);
   return q;
 }
-static float shrink_tiny(float a, float den, float rinv) {
+__attribute__((noinline)) static float shrink_tiny(float a, float den, float rinv) {
   const float a2 = a * 0x1p64f;
   const float q0 = a2 * rinv;
   const float q2 = fmaf(fmaf(-q0, den, a2), rinv, q0);
@@ -43,13 +47,19 @@ int main(int argc, char **argv) {
     int bad = 0;
     float r = shrink_fast(a, den, rinv, &bad);
     if (!bad) {
-      if (!(f2u(r) == f2u(ref) || (r != r && ref != ref))) ++bad_fast;
+      if (!(f2u(r) == f2u(ref) || (r != r && ref != ref))) {
+        ++bad_fast;
+        fprintf(stderr, "fast mismatch: a=%08x (%.9g) fast=%08x ieee=%08x\n", (unsigned)i, a, f2u(r), f2u(ref));
+      }
       continue;
     }
     if (a != 0.0f && fabsf(a) < 1.0e-30f) {
       ++n_tiny;
       r = shrink_tiny(a, den, rinv);
-      if (!(f2u(r) == f2u(ref))) ++bad_tiny;
+      if (!(f2u(r) == f2u(ref))) {
+        ++bad_tiny;
+        fprintf(stderr, "tiny mismatch: a=%08x (%.9g) fast=%08x ieee=%08x\n", (unsigned)i, a, f2u(r), f2u(ref));
+      }
     } else ++n_ieee;
   }
   printf("den=%.9g fast-mismatch=%llu tiny=%llu tiny-mismatch=%llu ieee=%llu\n", den, bad_fast, n_tiny, bad_tiny, n_ieee);

@@ -23,7 +23,7 @@ def checker(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("lam", ["0.05", "0.5", "7.5"])
+@pytest.mark.parametrize("lam", ["0.05", "7.5"])
 def test_shrink_division_exact_for_every_float(checker, lam):
     r = subprocess.run([checker, lam], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr

@@ -61,6 +61,32 @@ def test_forward_projection_bitexact(setup, orc):
         assert np.array_equal(host(img), oi)
 
 
+@pytest.mark.parametrize("n,bricks", [(32, 1), (37, 1), (37, 0)])
+def test_forward_projection_brick_layout_bitexact(wapmod, orc, torch_cuda, n, bricks):
+    """fp_bricks = 1 (the default): the projector reads a 4x4x4 brick-layout
+    copy of the volume (a ragged size pads the last bricks); fp_bricks = 0:
+    the linear volume.  Both give the oracle's bits."""
+    import oracle as O
+    torch = torch_cuda
+    d = 48
+    vol = P.ellipsoids(n, seed=6)
+    ang = P.golden_angles(6)
+    ctx = wapmod.Context(wapmod.make_scan((n, n, n), (d, d), 6), ang)
+    ctx.set_tuning("fp_bricks", bricks)
+    oscan = O.make_scan((n, n, n), (d, d), 6)
+    dvol = dev(torch, vol)
+    try:
+        for p in range(6):
+            img = torch.zeros((d, d), device="cuda")
+            ln, wt = torch.zeros_like(img), torch.zeros_like(img)
+            ctx.forward(p, dvol, img, ln, wt)
+            ctx.synchronize()
+            oi, ol, ow = orc.forward(oscan, ang[p], vol)
+            assert np.array_equal(host(wt), ow) and np.array_equal(host(ln), ol) and np.array_equal(host(img), oi), p
+    finally:
+        ctx.close()
+
+
 def test_forward_projection_config0_size(wapmod, orc, torch_cuda):
     import oracle as O
     torch = torch_cuda

@@ -205,6 +205,9 @@ struct wap_ctx {
   DevMem blur_a, blur_b, rs_a, rs_b;
   DevMem pyr_b1, pyr_b2;  // blurred full-size flow inputs
   DevMem adv_tab;         // cell-centre table of a wap_advect call
+  DevMem bricks;          // brick-layout copies of the volumes a projection batch reads
+  DevMem jobs_fpb;        // the batch's projection jobs pointing at those copies
+  int fp_bricks = 1;      // 1: the forward projector reads brick-layout copies (same bits, faster)
   std::map<std::pair<int, int>, std::unique_ptr<DevMem[]>> resize_tables;
   DevMem cg_buf;
 
@@ -343,14 +346,31 @@ int sart_frames(wap_ctx *ctx, const std::vector<int> &frames, int nb_sart, const
     }
   }
   step_off[maxnum] = (int)fp.size();
+  // Brick layout: each step projects brick copies, made from the volumes the
+  // previous step's backprojection just updated (jobs_fp keeps the linear
+  // volumes for the conversion, jobs_fpb points at the copies).
+  const bool bricks = ctx->fp_bricks != 0;
+  const size_t bf = brick_floats(ctx->scan.vol);
+  if (bricks) {
+    int maxn = 0;
+    for (int s = 0; s < maxnum; ++s) maxn = std::max(maxn, step_off[s + 1] - step_off[s]);
+    CU(ctx->bricks.ensure(sizeof(float) * bf * maxn));
+    std::vector<FpJob> fpb = fp;
+    for (int s = 0; s < maxnum; ++s)
+      for (int q = step_off[s]; q < step_off[s + 1]; ++q) fpb[q].vol = ctx->bricks.as<float>() + (q - step_off[s]) * bf;
+    TRY(upload(ctx, ctx->jobs_fpb, fpb));
+  }
   TRY(upload(ctx, ctx->jobs_fp, fp));
   TRY(upload(ctx, ctx->jobs_bp, bp));
   int mb[3] = {box[1] - box[0], box[3] - box[2], box[5] - box[4]};
   for (int it = 1; it <= nb_sart; ++it)
     for (int s = 0; s < maxnum; ++s) {
       const int n = step_off[s + 1] - step_off[s];
-      KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_fp.as<FpJob>() + step_off[s], n, ctx->scan.vol, W, H,
-                        ctx->sd, ctx->scan.alpha, ctx->stream));
+      if (bricks)
+        KL(launch_brick_jobs(ctx->jobs_fp.as<FpJob>() + step_off[s], n, ctx->bricks.as<float>(), ctx->scan.vol,
+                             ctx->stream));
+      KL(launch_forward(ctx->geom.as<ProjGeom>(), (bricks ? ctx->jobs_fpb : ctx->jobs_fp).as<FpJob>() + step_off[s],
+                        n, ctx->scan.vol, W, H, ctx->sd, ctx->scan.alpha, ctx->stream, bricks));
       ctx->stats.fp_launches++;
       ctx->stats.projections += n;
       ctx->stats.backprojections += n;
@@ -431,9 +451,18 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
   TRY(upload(ctx, ctx->jobs_acc, acc));
   const int n = (int)items.size();
   const bool fast = ctx->flow_bits == 16;  // the precision form's warps
+  const bool bricks = ctx->fp_bricks != 0;
+  if (bricks) {  // the projector reads brick copies of the warped volumes
+    const size_t bf = brick_floats(d);
+    CU(ctx->bricks.ensure(sizeof(float) * bf * n));
+    std::vector<FpJob> fpb = fp;
+    for (int q = 0; q < n; ++q) fpb[q].vol = ctx->bricks.as<float>() + q * bf;
+    TRY(upload(ctx, ctx->jobs_fpb, fpb));
+  }
   KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>(), n, 1, ctx->stream, fast));
-  KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_fp.as<FpJob>(), n, d, W, H, ctx->sd, ctx->scan.alpha,
-                    ctx->stream));
+  if (bricks) KL(launch_brick_jobs(ctx->jobs_fp.as<FpJob>(), n, ctx->bricks.as<float>(), d, ctx->stream));
+  KL(launch_forward(ctx->geom.as<ProjGeom>(), (bricks ? ctx->jobs_fpb : ctx->jobs_fp).as<FpJob>(), n, d, W, H, ctx->sd,
+                    ctx->scan.alpha, ctx->stream, bricks));
   ctx->stats.fp_launches++;
   for (const WapItem &it : items)
     CU(cudaMemsetAsync(ctx->delta.as<float>() + (size_t)it.frame * nv, 0, sizeof(float) * nv, ctx->stream));
@@ -1212,6 +1241,10 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
     CHECK(value == 32 || value == 16, WAP_EINVAL, "flow_bits must be 32 or 16");
     ctx->flow_bits = value;
     return WAP_OK;
+  } else if (k == "fp_bricks") {
+    CHECK(value == 0 || value == 1, WAP_EINVAL, "fp_bricks must be 0 or 1");
+    ctx->fp_bricks = value;
+    return WAP_OK;
   } else if (k == "pd_zchunk") {
     CHECK(value >= 0, WAP_EINVAL, "pd_zchunk must be >= 0");
     ctx->pd_zchunk = value;
@@ -1397,11 +1430,18 @@ int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const 
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(njobs >= 1 && njobs <= 65535, WAP_EINVAL, "job count out of range");
   std::vector<FpJob> jobs(njobs);
+  const size_t bf = brick_floats(ctx->scan.vol);
+  if (ctx->fp_bricks) CU(ctx->bricks.ensure(sizeof(float) * bf * njobs));
   for (int q = 0; q < njobs; ++q) {
     CHECK(h_proj[q] >= 0 && h_proj[q] < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
     CHECK(h_d_vols[q], WAP_EINVAL, "null volume");
     FpJob j{};
     j.vol = h_d_vols[q];
+    if (ctx->fp_bricks) {  // the projector reads a brick-layout copy
+      float *b = ctx->bricks.as<float>() + (size_t)q * bf;
+      KL(launch_brick(h_d_vols[q], b, ctx->scan.vol, ctx->stream));
+      j.vol = b;
+    }
     j.proj = h_proj[q];
     j.img = h_d_imgs ? h_d_imgs[q] : nullptr;
     j.len = h_d_lens ? h_d_lens[q] : nullptr;
@@ -1410,7 +1450,7 @@ int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const 
   }
   TRY(upload(ctx, ctx->jobs_misc, jobs));
   KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_misc.as<FpJob>(), njobs, ctx->scan.vol, ctx->scan.det[0],
-                    ctx->scan.det[1], ctx->sd, ctx->scan.alpha, ctx->stream));
+                    ctx->scan.det[1], ctx->sd, ctx->scan.alpha, ctx->stream, ctx->fp_bricks != 0));
   ctx->stats.fp_launches++;
   return WAP_OK;
 }
@@ -1612,7 +1652,7 @@ size_t wap_ctx_device_bytes(const wap_ctx *ctx) {
                           &ctx->xprev, &ctx->zero_vol, &ctx->dual, &ctx->corr, &ctx->warped, &ctx->delta, &ctx->back,
                           &ctx->jobs_fp, &ctx->jobs_bp, &ctx->jobs_adv, &ctx->jobs_acc, &ctx->jobs_misc, &ctx->world,
                           &ctx->maxbits, &ctx->blur_a, &ctx->blur_b, &ctx->rs_a, &ctx->rs_b, &ctx->cg_buf,
-                          &ctx->pyr_b1, &ctx->pyr_b2, &ctx->adv_tab})
+                          &ctx->pyr_b1, &ctx->pyr_b2, &ctx->adv_tab, &ctx->bricks, &ctx->jobs_fpb})
     b += m->want;
   for (const auto &kv : ctx->flow_work) {
     const FlowWork &w = *kv.second;
@@ -1654,6 +1694,7 @@ size_t wap_job_device_bytes(const wap_scan_desc *scan, const wap_schedule *sch) 
     t_eta *= sch->flow_eta;
   }
   floats += 24 * nv;
+  floats += (size_t)F * brick_floats(scan->vol);  // brick copies for the projector, one per frame of a batch
   const size_t tables = (size_t)scan->nproj * sizeof(ProjGeom) + (size_t)4 * 1024 * 1024;  // geometry, job tables
   return floats * sizeof(float) + tables;
 }

@@ -11,6 +11,7 @@
 // reformulated.  Each warp owns an 8x4 pixel patch so the warp's 32 rays stay
 // within a few voxels of each other and the trilinear gathers hit L1.
 #include <cstring>
+#include <type_traits>
 
 #include "wap_internal.h"
 
@@ -29,9 +30,26 @@ struct VolView {
   }
 };
 
+// The same volume as 4x4x4 bricks of 64 floats (bricks x-fastest, each brick
+// z-major inside), so the 32 rays of a warp, which sample a small patch of a
+// plane across the ray direction, gather from a few 256-byte bricks instead
+// of many x rows.  Same clamping, same values: only the address changes.
+struct BrickView {
+  const float *__restrict__ d;
+  int nx, ny, nz, nbx, nby;
+  __device__ __forceinline__ float at(int x, int y, int z) const {
+    x = mac_maxi(mac_mini(x, nx - 1), 0);
+    y = mac_maxi(mac_mini(y, ny - 1), 0);
+    z = mac_maxi(mac_mini(z, nz - 1), 0);
+    const int b = ((z >> 2) * nby + (y >> 2)) * nbx + (x >> 2);
+    return __ldg(d + ((size_t)b << 6) + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3));
+  }
+};
+
 // Trilinear sample with the reference's clamp-then-truncate (SingleScalarVolume.core.h:99-202).
+template <class View>
 struct TrilinearSampler {
-  VolView v;
+  View v;
   float sumw;
   __device__ __forceinline__ float operator()(float p0, float p1, float p2) {
     p0 = mac_max(mac_min(p0, (float)(v.nx - 1)), 0.0f);
@@ -166,6 +184,30 @@ __device__ __forceinline__ float cast_ray(Sampler &smp, const int n[3], const fl
   return density;
 }
 
+// Linear (x-fastest) volume -> the BrickView layout; cells of partial bricks
+// past the grid are never read (indices are clamped first).
+__global__ void brick_kernel(const float *__restrict__ in, float *__restrict__ out, int nx, int ny, int nz) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)nx * ny * nz) return;
+  const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((size_t)nx * ny));
+  const int nbx = (nx + 3) >> 2, nby = (ny + 3) >> 2;
+  const int b = ((z >> 2) * nby + (y >> 2)) * nbx + (x >> 2);
+  out[((size_t)b << 6) + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3)] = in[i];
+}
+
+// The volumes of n projection jobs (jobs[j].vol, linear) into consecutive
+// brick-layout slots of bf floats; blockIdx.y is the job.
+__global__ void brick_jobs_kernel(const FpJob *__restrict__ jobs, float *__restrict__ out, size_t bf, int nx, int ny,
+                                  int nz) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i >= (size_t)nx * ny * nz) return;
+  const float *in = jobs[blockIdx.y].vol;
+  const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((size_t)nx * ny));
+  const int nbx = (nx + 3) >> 2, nby = (ny + 3) >> 2;
+  const int b = ((z >> 2) * nby + (y >> 2)) * nbx + (x >> 2);
+  out[blockIdx.y * bf + ((size_t)b << 6) + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3)] = in[i];
+}
+
 // 16x8 pixel tile per 128-thread block, each warp an 8x4 patch.
 __device__ __forceinline__ void tile_pixel(int &i, int &j) {
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
@@ -173,6 +215,7 @@ __device__ __forceinline__ void tile_pixel(int &i, int &j) {
   j = blockIdx.y * 8 + (w >> 1) * 4 + (lane >> 3);
 }
 
+template <class View>
 __global__ void __launch_bounds__(128) fp_kernel(const ProjGeom *__restrict__ geom, const FpJob *__restrict__ jobs,
                                                  int nx, int ny, int nz, int W, int H, float sd, double alpha) {
   int i, j;
@@ -183,7 +226,12 @@ __global__ void __launch_bounds__(128) fp_kernel(const ProjGeom *__restrict__ ge
   const int n[3] = {nx, ny, nz};
   float vz[4], vu[4], tn, tf;
   produce_ray(g, nx, ny, nz, (float)i, (float)j, vz, vu, tn, tf);
-  TrilinearSampler smp{VolView{job.vol, nx, ny, nz}, 0.0f};
+  View view;
+  if constexpr (std::is_same<View, BrickView>::value)
+    view = BrickView{job.vol, nx, ny, nz, (nx + 3) >> 2, (ny + 3) >> 2};
+  else
+    view = VolView{job.vol, nx, ny, nz};
+  TrilinearSampler<View> smp{view, 0.0f};
   float value = 0.0f, len = 0.0f;
   if (tn < tf) {
     len = tf - tn;
@@ -329,10 +377,30 @@ __global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restric
 }  // namespace
 
 cudaError_t launch_forward(const ProjGeom *d_geom, const FpJob *d_jobs, int njobs, const int dims[3], int W, int H,
-                           float sd, double alpha, cudaStream_t st) {
+                           float sd, double alpha, cudaStream_t st, bool bricked) {
   if (njobs <= 0) return cudaSuccess;
   dim3 grid((W + 15) / 16, (H + 7) / 8, njobs);
-  fp_kernel<<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
+  if (bricked) fp_kernel<BrickView><<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
+  else fp_kernel<VolView><<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
+  return cudaGetLastError();
+}
+
+size_t brick_floats(const int dims[3]) {
+  return (size_t)((dims[0] + 3) >> 2) * ((dims[1] + 3) >> 2) * ((dims[2] + 3) >> 2) * 64;
+}
+
+cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const int dims[3], cudaStream_t st) {
+  const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
+  if (nv == 0 || njobs <= 0) return cudaSuccess;
+  const dim3 g((unsigned)((nv + 255) / 256), (unsigned)njobs);
+  brick_jobs_kernel<<<g, 256, 0, st>>>(d_jobs, out, brick_floats(dims), dims[0], dims[1], dims[2]);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_brick(const float *vol, float *out, const int dims[3], cudaStream_t st) {
+  const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
+  if (nv == 0) return cudaSuccess;
+  brick_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(vol, out, dims[0], dims[1], dims[2]);
   return cudaGetLastError();
 }
 

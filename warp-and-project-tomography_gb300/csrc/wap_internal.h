@@ -75,8 +75,16 @@ struct SplatJob {
 };
 
 // Launch helpers (implemented in the .cu files).
+// bricked: the jobs' volumes are in the 4x4x4 brick layout (launch_brick).
 cudaError_t launch_forward(const ProjGeom *d_geom, const FpJob *d_jobs, int njobs, const int dims[3], int W, int H,
-                           float sd, double alpha, cudaStream_t st);
+                           float sd, double alpha, cudaStream_t st, bool bricked = false);
+// Floats of a volume's brick layout (dims rounded up to multiples of 4), and
+// the conversion of a linear volume into it.
+size_t brick_floats(const int dims[3]);
+cudaError_t launch_brick(const float *vol, float *out, const int dims[3], cudaStream_t st);
+// The volumes of njobs projection jobs (d_jobs[j].vol) into slots j of out
+// (brick_floats(dims) floats apart), one launch (njobs <= 65535).
+cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const int dims[3], cudaStream_t st);
 cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njobs, int maxbox[3], const int dims[3],
                             int W, int H, double halfW, double halfH, float sdd, double ds, double alpha, float gmax,
                             int mode, int exact, cudaStream_t st);

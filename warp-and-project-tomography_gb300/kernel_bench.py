@@ -39,6 +39,7 @@ def main():
     ap.add_argument("--pd-form", type=int, default=0, help="0 autotuned, 1 fused, 2 primal+dual, 3 TMA-fed fused")
     ap.add_argument("--pd-zchunk", type=int, default=0)
     ap.add_argument("--flow-bits", type=int, default=32, help="16: the precision form (FP16 flow state)")
+    ap.add_argument("--fp-bricks", type=int, default=0, help="1: the projector reads a brick-layout volume copy")
     a = ap.parse_args()
     build.build()
     n, d = a.n, a.det
@@ -79,6 +80,7 @@ def main():
         vol = torch.rand((n, n, n), device="cuda", generator=g)
         projs = torch.rand((16, d, d), device="cuda", generator=g)
     ctx.set_projections_device(projs)
+    ctx.set_tuning("fp_bricks", a.fp_bricks)
     if a.kernel in ("fp", "all"):
         img = torch.zeros((d, d), device="cuda")
         wt = torch.zeros_like(img)
