@@ -14,10 +14,7 @@
 #include <stdlib.h>
 static float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
 static uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
-/* noinline: each candidate is evaluated as the scalar sequence written here;
- * inlined into the OpenMP loop, GCC on aarch64 vectorised the loop and one
- * input (a = -0) then came out as +0, while the same sequence compiled on its
- * own gives -0 there as on x86 and on the GPU. */
+/* noinline: each candidate is evaluated as the scalar sequence written here. */
 __attribute__((noinline)) static float shrink_fast(float a, float den, float rinv, int *bad) {
   const float q0 = a * rinv;
   const float en = fmaf(q0, den, -a);

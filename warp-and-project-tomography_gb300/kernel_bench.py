@@ -39,7 +39,7 @@ def main():
     ap.add_argument("--pd-form", type=int, default=0, help="0 autotuned, 1 fused, 2 primal+dual, 3 TMA-fed fused")
     ap.add_argument("--pd-zchunk", type=int, default=0)
     ap.add_argument("--flow-bits", type=int, default=32, help="16: the precision form (FP16 flow state)")
-    ap.add_argument("--fp-bricks", type=int, default=0, help="1: the projector reads a brick-layout volume copy")
+    ap.add_argument("--fp-bricks", type=int, default=1, help="0: the projector reads the linear volume (1: brick-layout copy)")
     a = ap.parse_args()
     build.build()
     n, d = a.n, a.det
