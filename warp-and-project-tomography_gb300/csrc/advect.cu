@@ -110,6 +110,60 @@ __device__ __forceinline__ float sample(const float *__restrict__ img, const Gri
   return std_max(mn, std_min(mx, c));
 }
 
+// The three velocity channels at one located point: the same taps, limiter
+// and arithmetic per channel as three sample() calls, in one pass over the
+// taps so the index arithmetic is shared and the channels' loads interleave.
+template <bool FAST>
+__device__ __forceinline__ void sample3(const float *__restrict__ vel, size_t nv, const Grid3 &G,
+                                        const SamplePoint &s, float out[3]) {
+  const int nx = G.n[0], nxy = G.n[0] * G.n[1];
+  auto at = [&](int x, int y, int z) { return x + nx * y + nxy * z; };
+  float mn[3], mx[3];
+  {
+    const int i0 = at(s.ix, s.iy, s.iz);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) mn[c] = mx[c] = __ldg(vel + c * nv + i0);
+  }
+  const int o[7][3] = {{1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+#pragma unroll
+  for (int q = 0; q < 7; ++q) {
+    const int i = at(s.ix + o[q][0], s.iy + o[q][1], s.iz + o[q][2]);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float v = __ldg(vel + c * nv + i);
+      mn[c] = std_min(mn[c], v);
+      mx[c] = std_max(mx[c], v);
+    }
+  }
+  float p[3][4];
+#pragma unroll 1
+  for (int kz = 0; kz < 4; ++kz) {
+    const int z = kz == 0 ? s.zs[0] : kz == 1 ? s.zs[1] : kz == 2 ? s.zs[2] : s.zs[3];
+    float rows[3][4];
+#pragma unroll
+    for (int ky = 0; ky < 4; ++ky) {
+      const int r = at(0, s.ys[ky], z);
+      const int i0 = r + s.xs[0], i1 = r + s.xs[1], i2 = r + s.xs[2], i3 = r + s.xs[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float *ch = vel + c * nv;
+        rows[c][ky] = cubf<FAST>(__ldg(ch + i0), __ldg(ch + i1), __ldg(ch + i2), __ldg(ch + i3), s.dx);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float pl = cubf<FAST>(rows[c][0], rows[c][1], rows[c][2], rows[c][3], s.dy);
+      p[c][0] = kz == 0 ? pl : p[c][0];
+      p[c][1] = kz == 1 ? pl : p[c][1];
+      p[c][2] = kz == 2 ? pl : p[c][2];
+      p[c][3] = kz == 3 ? pl : p[c][3];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+    out[c] = std_max(mn[c], std_min(mx[c], cubf<FAST>(p[c][0], p[c][1], p[c][2], p[c][3], s.dz)));
+}
+
 template <bool FAST>
 __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__restrict__ wx,
                                                      const float *__restrict__ wy, const float *__restrict__ wz,
@@ -127,13 +181,12 @@ __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__
   const float p[3] = {__ldg(wx + i), __ldg(wy + j), __ldg(wz + k)};
   // trace (advection.h:101-115) with dt_trace = -dt.
   SamplePoint s = locate(G, p[0], p[1], p[2]);
-  float v0 = sample<FAST>(vel, G, s), v1 = sample<FAST>(vel + nv, G, s), v2 = sample<FAST>(vel + 2 * nv, G, s);
-  const float p2[3] = {p[0] + tdt * v0, p[1] + tdt * v1, p[2] + tdt * v2};
+  float v[3];
+  sample3<FAST>(vel, nv, G, s, v);
+  const float p2[3] = {p[0] + tdt * v[0], p[1] + tdt * v[1], p[2] + tdt * v[2]};
   s = locate(G, p2[0], p2[1], p2[2]);
-  v0 = sample<FAST>(vel, G, s);
-  v1 = sample<FAST>(vel + nv, G, s);
-  v2 = sample<FAST>(vel + 2 * nv, G, s);
-  const float p0[3] = {p2[0] - tdt * v0, p2[1] - tdt * v1, p2[2] - tdt * v2};
+  sample3<FAST>(vel, nv, G, s, v);
+  const float p0[3] = {p2[0] - tdt * v[0], p2[1] - tdt * v[1], p2[2] - tdt * v[2]};
   const float q[3] = {p2[0] + (p[0] - p0[0]) * 0.5f, p2[1] + (p[1] - p0[1]) * 0.5f, p2[2] + (p[2] - p0[2]) * 0.5f};
   s = locate(G, q[0], q[1], q[2]);
   const size_t o = i + (size_t)G.n[0] * (j + (size_t)G.n[1] * k);
