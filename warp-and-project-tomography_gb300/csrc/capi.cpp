@@ -265,6 +265,14 @@ int upload(wap_ctx *ctx, DevMem &m, const std::vector<T> &h) {
   return WAP_OK;
 }
 
+// Room for brick-layout copies of `floats` floats; without it (device memory
+// exhausted) the projector reads the linear volumes, which gives the same bits.
+bool brick_room(wap_ctx *ctx, size_t floats) {
+  if (ctx->bricks.ensure(sizeof(float) * floats) == cudaSuccess) return true;
+  cudaGetLastError();
+  return false;
+}
+
 float *vol_ptr(wap_ctx *c, int f) { return c->vols.as<float>() + (size_t)f * c->nv; }
 float *flow_ptr(wap_ctx *c, int f) { return c->flows.as<float>() + (size_t)f * 3 * c->nv; }
 
@@ -349,12 +357,11 @@ int sart_frames(wap_ctx *ctx, const std::vector<int> &frames, int nb_sart, const
   // Brick layout: each step projects brick copies, made from the volumes the
   // previous step's backprojection just updated (jobs_fp keeps the linear
   // volumes for the conversion, jobs_fpb points at the copies).
-  const bool bricks = ctx->fp_bricks != 0;
   const size_t bf = brick_floats(ctx->scan.vol);
+  int maxn = 0;
+  for (int s = 0; s < maxnum; ++s) maxn = std::max(maxn, step_off[s + 1] - step_off[s]);
+  const bool bricks = ctx->fp_bricks != 0 && brick_room(ctx, bf * maxn);
   if (bricks) {
-    int maxn = 0;
-    for (int s = 0; s < maxnum; ++s) maxn = std::max(maxn, step_off[s + 1] - step_off[s]);
-    CU(ctx->bricks.ensure(sizeof(float) * bf * maxn));
     std::vector<FpJob> fpb = fp;
     for (int s = 0; s < maxnum; ++s)
       for (int q = step_off[s]; q < step_off[s + 1]; ++q) fpb[q].vol = ctx->bricks.as<float>() + (q - step_off[s]) * bf;
@@ -451,10 +458,9 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
   TRY(upload(ctx, ctx->jobs_acc, acc));
   const int n = (int)items.size();
   const bool fast = ctx->flow_bits == 16;  // the precision form's warps
-  const bool bricks = ctx->fp_bricks != 0;
+  const size_t bf = brick_floats(d);
+  const bool bricks = ctx->fp_bricks != 0 && brick_room(ctx, bf * n);
   if (bricks) {  // the projector reads brick copies of the warped volumes
-    const size_t bf = brick_floats(d);
-    CU(ctx->bricks.ensure(sizeof(float) * bf * n));
     std::vector<FpJob> fpb = fp;
     for (int q = 0; q < n; ++q) fpb[q].vol = ctx->bricks.as<float>() + q * bf;
     TRY(upload(ctx, ctx->jobs_fpb, fpb));
@@ -1431,13 +1437,13 @@ int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const 
   CHECK(njobs >= 1 && njobs <= 65535, WAP_EINVAL, "job count out of range");
   std::vector<FpJob> jobs(njobs);
   const size_t bf = brick_floats(ctx->scan.vol);
-  if (ctx->fp_bricks) CU(ctx->bricks.ensure(sizeof(float) * bf * njobs));
+  const bool bricks = ctx->fp_bricks != 0 && brick_room(ctx, bf * njobs);
   for (int q = 0; q < njobs; ++q) {
     CHECK(h_proj[q] >= 0 && h_proj[q] < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
     CHECK(h_d_vols[q], WAP_EINVAL, "null volume");
     FpJob j{};
     j.vol = h_d_vols[q];
-    if (ctx->fp_bricks) {  // the projector reads a brick-layout copy
+    if (bricks) {  // the projector reads a brick-layout copy
       float *b = ctx->bricks.as<float>() + (size_t)q * bf;
       KL(launch_brick(h_d_vols[q], b, ctx->scan.vol, ctx->stream));
       j.vol = b;
@@ -1450,7 +1456,7 @@ int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const 
   }
   TRY(upload(ctx, ctx->jobs_misc, jobs));
   KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_misc.as<FpJob>(), njobs, ctx->scan.vol, ctx->scan.det[0],
-                    ctx->scan.det[1], ctx->sd, ctx->scan.alpha, ctx->stream, ctx->fp_bricks != 0));
+                    ctx->scan.det[1], ctx->sd, ctx->scan.alpha, ctx->stream, bricks));
   ctx->stats.fp_launches++;
   return WAP_OK;
 }
