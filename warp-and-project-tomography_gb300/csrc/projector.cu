@@ -184,28 +184,43 @@ __device__ __forceinline__ float cast_ray(Sampler &smp, const int n[3], const fl
   return density;
 }
 
-// Linear (x-fastest) volume -> the BrickView layout; cells of partial bricks
-// past the grid are never read (indices are clamped first).
-__global__ void brick_kernel(const float *__restrict__ in, float *__restrict__ out, int nx, int ny, int nz) {
-  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= (size_t)nx * ny * nz) return;
-  const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((size_t)nx * ny));
+// Linear (x-fastest) volume -> the BrickView layout.  A 256-thread block
+// moves a 32 x 4 x 4 tile: eight x-consecutive bricks, which are 2 KB in a
+// row of the output, so the rows of the tile are read and the bricks written
+// with whole-line accesses through shared memory.  Cells of partial bricks
+// past the grid are written as 0 and never read (indices are clamped first).
+__device__ __forceinline__ void brick_tile(const float *__restrict__ in, float *__restrict__ out, int nx, int ny,
+                                           int nz, int x0, int y0, int z0, float (*t)[4][32]) {
+  const int tid = threadIdx.x;
+  for (int e = tid; e < 512; e += 256) {  // rows in: e = (z * 4 + y) * 32 + x
+    const int x = e & 31, y = (e >> 5) & 3, z = e >> 7;
+    const int gx = x0 + x, gy = y0 + y, gz = z0 + z;
+    t[z][y][x] = (gx < nx && gy < ny && gz < nz) ? in[gx + (size_t)nx * (gy + (size_t)ny * gz)] : 0.0f;
+  }
+  __syncthreads();
   const int nbx = (nx + 3) >> 2, nby = (ny + 3) >> 2;
-  const int b = ((z >> 2) * nby + (y >> 2)) * nbx + (x >> 2);
-  out[((size_t)b << 6) + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3)] = in[i];
+  const size_t b0 = ((size_t)(z0 >> 2) * nby + (y0 >> 2)) * nbx + (x0 >> 2);
+  for (int o = tid; o < 512; o += 256) {  // bricks out: o = brick * 64 + (z * 4 + y) * 4 + x
+    const int bx = o >> 6;
+    if ((x0 >> 2) + bx >= nbx) continue;
+    const int x = (o & 3) + 4 * bx, y = (o >> 2) & 3, z = (o >> 4) & 3;
+    out[(b0 << 6) + o] = t[z][y][x];
+  }
+}
+
+__global__ void __launch_bounds__(256) brick_kernel(const float *__restrict__ in, float *__restrict__ out, int nx,
+                                                    int ny, int nz) {
+  __shared__ float t[4][4][32];
+  brick_tile(in, out, nx, ny, nz, blockIdx.x * 32, blockIdx.y * 4, blockIdx.z * 4, t);
 }
 
 // The volumes of n projection jobs (jobs[j].vol, linear) into consecutive
-// brick-layout slots of bf floats; blockIdx.y is the job.
-__global__ void brick_jobs_kernel(const FpJob *__restrict__ jobs, float *__restrict__ out, size_t bf, int nx, int ny,
-                                  int nz) {
-  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (i >= (size_t)nx * ny * nz) return;
-  const float *in = jobs[blockIdx.y].vol;
-  const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((size_t)nx * ny));
-  const int nbx = (nx + 3) >> 2, nby = (ny + 3) >> 2;
-  const int b = ((z >> 2) * nby + (y >> 2)) * nbx + (x >> 2);
-  out[blockIdx.y * bf + ((size_t)b << 6) + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3)] = in[i];
+// brick-layout slots of bf floats; blockIdx.z runs over z tiles x jobs.
+__global__ void __launch_bounds__(256) brick_jobs_kernel(const FpJob *__restrict__ jobs, float *__restrict__ out,
+                                                         size_t bf, int nx, int ny, int nz, int ztiles) {
+  __shared__ float t[4][4][32];
+  const int j = blockIdx.z / ztiles;
+  brick_tile(jobs[j].vol, out + j * bf, nx, ny, nz, blockIdx.x * 32, blockIdx.y * 4, (blockIdx.z % ztiles) * 4, t);
 }
 
 // 16x8 pixel tile per 128-thread block, each warp an 8x4 patch.
@@ -390,17 +405,19 @@ size_t brick_floats(const int dims[3]) {
 }
 
 cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const int dims[3], cudaStream_t st) {
-  const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
-  if (nv == 0 || njobs <= 0) return cudaSuccess;
-  const dim3 g((unsigned)((nv + 255) / 256), (unsigned)njobs);
-  brick_jobs_kernel<<<g, 256, 0, st>>>(d_jobs, out, brick_floats(dims), dims[0], dims[1], dims[2]);
+  if ((size_t)dims[0] * dims[1] * dims[2] == 0 || njobs <= 0) return cudaSuccess;
+  const int ztiles = (dims[2] + 3) / 4;
+  if ((long long)ztiles * njobs > 65535 || (dims[1] + 3) / 4 > 65535) return cudaErrorInvalidValue;
+  const dim3 g((unsigned)((dims[0] + 31) / 32), (unsigned)((dims[1] + 3) / 4), (unsigned)(ztiles * njobs));
+  brick_jobs_kernel<<<g, 256, 0, st>>>(d_jobs, out, brick_floats(dims), dims[0], dims[1], dims[2], ztiles);
   return cudaGetLastError();
 }
 
 cudaError_t launch_brick(const float *vol, float *out, const int dims[3], cudaStream_t st) {
-  const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
-  if (nv == 0) return cudaSuccess;
-  brick_kernel<<<(unsigned)((nv + 255) / 256), 256, 0, st>>>(vol, out, dims[0], dims[1], dims[2]);
+  if ((size_t)dims[0] * dims[1] * dims[2] == 0) return cudaSuccess;
+  if ((dims[2] + 3) / 4 > 65535 || (dims[1] + 3) / 4 > 65535) return cudaErrorInvalidValue;
+  const dim3 g((unsigned)((dims[0] + 31) / 32), (unsigned)((dims[1] + 3) / 4), (unsigned)((dims[2] + 3) / 4));
+  brick_kernel<<<g, 256, 0, st>>>(vol, out, dims[0], dims[1], dims[2]);
   return cudaGetLastError();
 }
 
