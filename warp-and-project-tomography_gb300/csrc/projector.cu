@@ -44,6 +44,25 @@ struct BrickView {
     const int b = ((z >> 2) * nby + (y >> 2)) * nbx + (x >> 2);
     return __ldg(d + ((size_t)b << 6) + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3));
   }
+  // The 8 trilinear taps of cell (i, j, k), 0 <= i < nx etc., in the
+  // sampler's order, each index +1 clamped to n-1 as at() would: one brick
+  // address and a step per axis (within the brick, into the next brick, or 0
+  // at the last cell).
+  __device__ __forceinline__ void taps8(int i, int j, int k, float t[8]) const {
+    const size_t b = ((size_t)(k >> 2) * nby + (j >> 2)) * nbx + (i >> 2);
+    const float *p = d + (b << 6) + ((k & 3) << 4) + ((j & 3) << 2) + (i & 3);
+    const int sx = i + 1 > nx - 1 ? 0 : ((i & 3) == 3 ? 61 : 1);
+    const int sy = j + 1 > ny - 1 ? 0 : ((j & 3) == 3 ? nbx * 64 - 12 : 4);
+    const int sz = k + 1 > nz - 1 ? 0 : ((k & 3) == 3 ? nbx * nby * 64 - 48 : 16);
+    t[0] = __ldg(p);
+    t[1] = __ldg(p + sx);
+    t[2] = __ldg(p + sy);
+    t[3] = __ldg(p + sx + sy);
+    t[4] = __ldg(p + sz);
+    t[5] = __ldg(p + sx + sz);
+    t[6] = __ldg(p + sy + sz);
+    t[7] = __ldg(p + sx + sy + sz);
+  }
 };
 
 // Trilinear sample with the reference's clamp-then-truncate (SingleScalarVolume.core.h:99-202).
@@ -59,10 +78,23 @@ struct TrilinearSampler {
     float f2 = p0 - (float)i;
     float f1 = 1.0f - f2;
     sumw += 1.0f;
-    float a = v.at(i, j, k) * f1 + v.at(i + 1, j, k) * f2;
-    float b = v.at(i, j + 1, k) * f1 + v.at(i + 1, j + 1, k) * f2;
-    float c = v.at(i, j, k + 1) * f1 + v.at(i + 1, j, k + 1) * f2;
-    float d = v.at(i, j + 1, k + 1) * f1 + v.at(i + 1, j + 1, k + 1) * f2;
+    float tp[8];
+    if constexpr (std::is_same<View, BrickView>::value) {
+      v.taps8(i, j, k, tp);
+    } else {
+      tp[0] = v.at(i, j, k);
+      tp[1] = v.at(i + 1, j, k);
+      tp[2] = v.at(i, j + 1, k);
+      tp[3] = v.at(i + 1, j + 1, k);
+      tp[4] = v.at(i, j, k + 1);
+      tp[5] = v.at(i + 1, j, k + 1);
+      tp[6] = v.at(i, j + 1, k + 1);
+      tp[7] = v.at(i + 1, j + 1, k + 1);
+    }
+    float a = tp[0] * f1 + tp[1] * f2;
+    float b = tp[2] * f1 + tp[3] * f2;
+    float c = tp[4] * f1 + tp[5] * f2;
+    float d = tp[6] * f1 + tp[7] * f2;
     f2 = p1 - (float)j;
     f1 = 1.0f - f2;
     a = a * f1 + b * f2;
