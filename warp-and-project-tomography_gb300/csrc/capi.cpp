@@ -496,7 +496,16 @@ int resize_tables(wap_ctx *ctx, int Sin, int Sout, ResizeTables &tb) {
     TRY(upload(ctx, m[1], h.tap_src));
     TRY(upload(ctx, m[2], h.tap_w));
     TRY(upload(ctx, m[3], h.base));
-    TRY(upload(ctx, m[4], h.frac));
+    // per output: t, t*t and (t*t)*t, the products the cubic's double
+    // expression forms, computed once here in the same IEEE double
+    std::vector<double> f3(3 * h.frac.size());
+    for (size_t o = 0; o < h.frac.size(); ++o) {
+      const double t = h.frac[o], t2 = t * t;
+      f3[3 * o] = t;
+      f3[3 * o + 1] = t2;
+      f3[3 * o + 2] = t2 * t;
+    }
+    TRY(upload(ctx, m[4], f3));
     it = ctx->resize_tables.emplace(key, std::move(m)).first;
   }
   tb.tap_start = it->second[0].as<int>();

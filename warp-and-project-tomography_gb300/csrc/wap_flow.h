@@ -25,7 +25,7 @@ struct ResizeTables {
   const int *tap_src = nullptr;
   const float *tap_w = nullptr;
   const int *base = nullptr;       // Sout
-  const double *frac = nullptr;    // Sout
+  const double *frac = nullptr;    // 3 * Sout: t, t*t, t*t*t per output cell
 };
 
 DericheCoefs deriche_coefs(float sigma);
