@@ -37,17 +37,11 @@ struct VolView {
 struct BrickView {
   const float *__restrict__ d;
   int nx, ny, nz, nbx, nby;
-  __device__ __forceinline__ float at(int x, int y, int z) const {
-    x = mac_maxi(mac_mini(x, nx - 1), 0);
-    y = mac_maxi(mac_mini(y, ny - 1), 0);
-    z = mac_maxi(mac_mini(z, nz - 1), 0);
-    const int b = ((z >> 2) * nby + (y >> 2)) * nbx + (x >> 2);
-    return __ldg(d + ((size_t)b << 6) + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3));
-  }
   // The 8 trilinear taps of cell (i, j, k), 0 <= i < nx etc., in the
-  // sampler's order, each index +1 clamped to n-1 as at() would: one brick
-  // address and a step per axis (within the brick, into the next brick, or 0
-  // at the last cell).
+  // sampler's order, each index +1 clamped to n-1 as VolView::at does: one
+  // brick address (cell (x, y, z) sits at brick ((z/4) nby + y/4) nbx + x/4,
+  // offset 16 (z%4) + 4 (y%4) + x%4) and a step per axis (within the brick,
+  // into the next brick, or 0 at the last cell).
   __device__ __forceinline__ void taps8(int i, int j, int k, float t[8]) const {
     const size_t b = ((size_t)(k >> 2) * nby + (j >> 2)) * nbx + (i >> 2);
     const float *p = d + (b << 6) + ((k & 3) << 4) + ((j & 3) << 2) + (i & 3);
