@@ -313,7 +313,10 @@ WAP_API int wap_projection_geometry(const wap_scan_desc *scan, double angle_deg,
 /* image_cg::cg (cg.h:11-55) on A = a*I - b*Laplacian (Neumann): x updated in
  * place.  mode 0 is textbook CG; mode 1 reproduces the reference's update
  * (image_blas::add reassigns p before reading it, image_blas.h:135-149, so
- * p = r).  Dot products and norms in FP64.  Returns iterations in h_iters. */
+ * p = r).  Dot products and norms in FP64, summed in a fixed order, so a
+ * solve is reproducible bit for bit.  Returns iterations in h_iters (also on
+ * failure).  An error left pending by the caller's earlier CUDA work is
+ * reported as WAP_ECUDA before anything runs, and left pending. */
 WAP_API int wap_cg_screened_laplacian(wap_ctx *ctx, const int *dims, float a, float b, const float *d_rhs,
                                       float *d_x, float rel_tol, int max_iters, float abs_tol, int mode,
                                       int *h_iters);
@@ -323,13 +326,15 @@ WAP_API int wap_cg_screened_laplacian(wap_ctx *ctx, const int *dims, float a, fl
  * library allocate device memory: applications whose memory pool has reserved
  * the device, where an extra cudaMalloc fails, and serving loops that cannot
  * absorb the device-wide synchronisation of cudaFree.  Its scratch (the CG
- * vectors r, p, Ap plus FP64 accumulators) lives in one fixed device array of
- * 3 * WAP_CG_NOALLOC_MAX_VOXELS floats (3 MiB) + 256 bytes, which every GPU
- * that loads the library holds until the process exits.  Grids with more than
+ * vectors r, p, Ap, the FP64 per-block partial sums and four scalars) lives in
+ * one fixed device array of 3 * WAP_CG_NOALLOC_MAX_VOXELS floats (3 MiB) plus
+ * 16 KiB, which every GPU that loads the library holds until the process
+ * exits.  Grids with more than
  * WAP_CG_NOALLOC_MAX_VOXELS voxels return WAP_ETOOBIG.  It needs no context:
  * it works on the current device and orders its work on cuda_stream (NULL =
  * the legacy default stream), with the same arguments and results as
- * wap_cg_screened_laplacian.  The first call on each device looks the scratch
+ * wap_cg_screened_laplacian (bit for bit: both reduce in a fixed order).  The
+ * first call on each device looks the scratch
  * address up (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  Every call reuses the same scratch, so
  * calls that overlap on the GPU (other streams, other host threads) race. */

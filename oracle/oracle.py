@@ -23,7 +23,17 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libwaporacle.so")
 ORACLE64_SO = os.path.join(HERE, "_build", "libwaporacle64.so")
 REF_SO = os.path.join(HERE, "_ref", "libwapref.so")
-REF_TREE = os.environ.get("WAP_REFERENCE_TREE", "/root/reference")
+REF_TREE_FILE = os.path.join(HERE, "_ref", "tree.txt")
+
+
+def reference_tree():
+    """The reference source tree: $WAP_REFERENCE_TREE, else the tree the last
+    ``build_ref`` compiled (recorded in _ref/tree.txt), else None."""
+    t = os.environ.get("WAP_REFERENCE_TREE")
+    if not t and os.path.exists(REF_TREE_FILE):
+        with open(REF_TREE_FILE) as f:
+            t = f.read().strip()
+    return t if t and os.path.isdir(os.path.join(t, "Project")) else None
 
 _f32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _f64 = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -94,11 +104,15 @@ def build_oracle():
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
 
 
-def build_ref():
-    """Compile the reference's own sources (needs the reference tree)."""
-    if not os.path.isdir(os.path.join(REF_TREE, "Project")):
+def build_ref(tree=None):
+    """Compile the reference's own sources found in ``tree`` (default:
+    ``reference_tree()``) and record the tree for later calls."""
+    tree = tree or reference_tree()
+    if not tree or not os.path.isdir(os.path.join(tree, "Project")):
         return False
-    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + REF_TREE], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", HERE, "ref", "REF=" + tree], check=True)
+    with open(REF_TREE_FILE, "w") as f:
+        f.write(os.path.abspath(tree) + "\n")
     return True
 
 

@@ -2,8 +2,9 @@
 
 Runs the reference's own sources (compiled headless by `make -C oracle ref`
 into oracle/_ref/libwapref.so) on small seeded inputs and stores inputs and
-outputs as .npz files.  Needs the reference tree (default /root/reference,
-override with WAP_REFERENCE_TREE); the tests only read the .npz files.
+outputs as .npz files.  Needs oracle/_ref/libwapref.so, built from the
+reference tree by `make -C oracle ref REF=<tree>` (or by __graft_entry__.build()
+where the tree is present); the tests only read the .npz files.
 Single-threaded (OMP_NUM_THREADS=1) so the flow residual sums run in loop
 order.
 

@@ -8,6 +8,8 @@ import subprocess
 
 import pytest
 
+import oracle
+
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CLI = os.path.join(REPO, "warp-and-project-tomography_gb300", "lib", "wap_tomo")
 CHECK_SRC = os.path.join(REPO, "tests", "facade", "facade_check.cpp")
@@ -62,7 +64,8 @@ def test_facade_compiles_with_the_reference_signatures(tmp_path):
     inc = os.path.join(REPO, "include")
     r = run([gxx, "-std=c++17", "-fsyntax-only", "-I" + inc, CHECK_SRC])
     assert r.returncode == 0, r.stderr
-    ref = os.path.join(os.environ.get("WAP_REFERENCE_TREE", "/root/reference"), "Project")
-    if os.path.exists(os.path.join(ref, "CImg.h")):
+    tree = oracle.reference_tree()
+    ref = os.path.join(tree, "Project") if tree else ""
+    if tree and os.path.exists(os.path.join(ref, "CImg.h")):
         r = run([gxx, "-std=c++17", "-fsyntax-only", "-w", "-I" + inc, "-I" + ref, "-DWAP_WITH_CIMG", CHECK_SRC])
         assert r.returncode == 0, r.stderr

@@ -81,7 +81,7 @@ def test_create_without_gpu_or_with_bad_scan_fails_cleanly(wapmod):
 
 def test_reference_tree_live_pin(orc):
     """Where the reference tree exists, re-pin a forward projection live."""
-    if not os.path.isdir(os.path.join(O.REF_TREE, "Project")):
+    if not O.reference_tree() or not os.path.exists(O.REF_SO):
         pytest.skip("reference tree not present")
     import tempfile
     ref = O.Reference()
