@@ -161,6 +161,8 @@ class Oracle:
         _bind(L, "orc_cp_overrelax", None, [_i32, _i32, R, R, R])
         _bind(L, "orc_outer_iteration", _c_int, [S, ctypes.POINTER(Schedule), _f64, R, _c_int, R, R, R, R, R, R,
                                                  ctypes.POINTER(_c_int)])
+        _bind(L, "orc_outer_iteration_frames", _c_int, [S, ctypes.POINTER(Schedule), _f64, R, _c_int, _c_int,
+                                                        _c_int, R, R, R, R, R, R, ctypes.POINTER(_c_int)])
         _bind(L, "orc_cg_screened_laplacian", _c_int, [_i32, cR, cR, R, R, cR, _c_int, cR, _c_int])
 
     def arr(self, x):
@@ -257,6 +259,13 @@ class Oracle:
         F = self.lib.orc_outer_iteration(ctypes.byref(scan), ctypes.byref(sched), angles, projs, level,
                                          state["vols"], state["flows"], state["ytv"], state["ytp"], state["xbar"],
                                          state["xprev"], ctypes.byref(tot))
+        return F, tot.value
+
+    def outer_iteration_frames(self, scan, sched, angles, projs, level, f0, f1, state):
+        tot = _c_int()
+        F = self.lib.orc_outer_iteration_frames(ctypes.byref(scan), ctypes.byref(sched), angles, projs, level, f0,
+                                                f1, state["vols"], state["flows"], state["ytv"], state["ytp"],
+                                                state["xbar"], state["xprev"], ctypes.byref(tot))
         return F, tot.value
 
     def cg_screened_laplacian(self, dims, a, b, rhs, x, rel_tol=1e-6, max_iters=500, abs_tol=1e-9, mode=0):

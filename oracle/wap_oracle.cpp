@@ -1132,6 +1132,17 @@ void orc_cp_overrelax(const int dims[3], const int box[6], const real *vol, cons
 int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double *angles, const real *projs,
                         int level, real *vols, real *flows, real *ytv, real *ytp, real *xbar, real *xprev,
                         int *flow_iters_total) {
+  return orc_outer_iteration_frames(s, sch, angles, projs, level, 0, 1 << 30, vols, flows, ytv, ytp, xbar, xprev,
+                                    flow_iters_total);
+}
+
+// The outer iteration restricted to frames [f0, f1) (f1 clipped to F): their
+// CP + SART steps, the flows of the pairs (f, f+1) they start, their
+// warp-and-project windows; frames outside the range are read (CP neighbours,
+// the pair's second frame) but not updated.  [0, F) is one outer iteration.
+int orc_outer_iteration_frames(const orc_scan *s, const orc_schedule *sch, const double *angles, const real *projs,
+                               int level, int f0, int f1, real *vols, real *flows, real *ytv, real *ytp, real *xbar,
+                               real *xprev, int *flow_iters_total) {
   const int *d = s->vol;
   const size_t nv = (size_t)d[0] * d[1] * d[2];
   std::vector<int> st(130), en(130);
@@ -1144,8 +1155,9 @@ int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double
   const size_t np = (size_t)s->det[0] * s->det[1];
   std::vector<real> dual((size_t)s->nproj * np);
   std::vector<real> zero(nv, 0.0f);
+  f1 = std::min(f1, F);
   for (int icp = 1; icp <= sch->n_cp; ++icp)
-    for (int f = 0; f < F; ++f) {
+    for (int f = f0; f < f1; ++f) {
       const real *xb_next = (f + 1 < F) ? xbar + (f + 1) * nv : zero.data();
       orc_cp_dual(s, box, xbar + f * nv, xb_next, ytv + f * 3 * nv, ytp + f * nv);
       orc_cp_primal(s, box, f, f > 0 ? ytp + (f - 1) * nv : nullptr, ytp + f * nv, ytv + f * 3 * nv, vols + f * nv,
@@ -1155,7 +1167,7 @@ int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double
     }
   int total = 0;
   const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
-  for (int f = 0; f + 1 < F; ++f) {
+  for (int f = f0; f < f1 && f + 1 < F; ++f) {
     std::vector<real> out(3 * nv);
     total += orc_flow_multiscale(d, vols + f * nv, vols + (f + 1) * nv, flows + f * 3 * nv, sch->flow_tol,
                                  sch->flow_lambda, sch->flow_iters, sch->flow_warps, sch->flow_eta, sch->flow_sigma,
@@ -1163,7 +1175,7 @@ int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double
     std::memcpy(flows + f * 3 * nv, out.data(), 3 * nv * sizeof(real));
   }
   for (int wp = 0; wp < sch->nb_projwarp; ++wp)
-    for (int f = 0; f < sch->wp_frames && f < F; ++f)
+    for (int f = f0; f < sch->wp_frames && f < f1; ++f)
       for (int ik = st[f]; ik <= en[f]; ++ik) {
         real td = (ik - ft[f]) / tunit;
         td = mac_min(mac_max(-1.0f, td), 1.0f);

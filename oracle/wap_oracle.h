@@ -129,6 +129,11 @@ void orc_cp_overrelax(const int dims[3], const int box[6], const orc_real *vol, 
 int orc_outer_iteration(const orc_scan *s, const orc_schedule *sch, const double *angles, const orc_real *projs,
                         int level, orc_real *vols, orc_real *flows, orc_real *ytv, orc_real *ytp, orc_real *xbar, orc_real *xprev,
                         int *flow_iters_total);
+/* The same restricted to frames [f0, f1): their CP + SART steps, the flows of
+ * the pairs (f, f+1) they start and their warp-and-project windows. */
+int orc_outer_iteration_frames(const orc_scan *s, const orc_schedule *sch, const double *angles, const orc_real *projs,
+                               int level, int f0, int f1, orc_real *vols, orc_real *flows, orc_real *ytv,
+                               orc_real *ytp, orc_real *xbar, orc_real *xprev, int *flow_iters_total);
 
 /* image_cg::cg (cg.h:11-55) on A = a*I - b*Laplacian (clamped neighbours).
  * mode 0: textbook update p = r + beta*p; mode 1: the reference's aliasing
