@@ -13,6 +13,7 @@
 #include <cstring>
 #include <type_traits>
 
+#include "bp_cubic.h"
 #include "wap_internal.h"
 
 namespace wap {
@@ -367,7 +368,7 @@ __global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restric
                                                        int W, int H, double halfW, double halfH, float sdd,
                                                        double ds, int float_ok, double alpha, float gmax,
                                                        float halfWf, float halfHf, float dsf, float alphaf,
-                                                       float wlim, float hlim) {
+                                                       float alphal, float wlim, float hlim) {
   const int jb = blockIdx.z / zblocks;
   const BpJob job = jobs[jb];
   const int x = job.box[0] + blockIdx.x * blockDim.x + threadIdx.x;
@@ -396,18 +397,41 @@ __global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restric
   const int px = small_f2i(fx), py = small_f2i(fy);
   const float dx = _px - fx, dy = _py - fy;
   const float *__restrict__ pC = job.corr + py * W + px;
-  float arr[4];
+  float pv[4][4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const float *c = pC + (r - 1);
-    const float a0 = __ldg(c - W), a1 = __ldg(c), a2 = __ldg(c + W), a3 = __ldg(c + 2 * W);
-    arr[r] = kExact ? cubic_exact(a0, a1, a2, a3, dy) : cubic_fast(a0, a1, a2, a3, dy);
+    pv[r][0] = __ldg(c - W);
+    pv[r][1] = __ldg(c);
+    pv[r][2] = __ldg(c + W);
+    pv[r][3] = __ldg(c + 2 * W);
   }
-  const float gv = kExact ? cubic_exact(arr[0], arr[1], arr[2], arr[3], dx)
-                          : cubic_fast(arr[0], arr[1], arr[2], arr[3], dx);
+  float arr[4], gv;
+  if (kExact) {
+    // The reference's double arithmetic: certified float-float where the
+    // float result is certain (nearly always), the FP64 pipe otherwise.
+    bool ok = true;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) ok = bpc::cubic_cert(pv[r][0], pv[r][1], pv[r][2], pv[r][3], dy, &arr[r]) && ok;
+    ok = ok && bpc::cubic_cert(arr[0], arr[1], arr[2], arr[3], dx, &gv);
+    if (!ok) {
+#pragma unroll
+      for (int r = 0; r < 4; ++r) arr[r] = cubic_exact(pv[r][0], pv[r][1], pv[r][2], pv[r][3], dy);
+      gv = cubic_exact(arr[0], arr[1], arr[2], arr[3], dx);
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) arr[r] = cubic_fast(pv[r][0], pv[r][1], pv[r][2], pv[r][3], dy);
+    gv = cubic_fast(arr[0], arr[1], arr[2], arr[3], dx);
+  }
   float *v = job.vol + (x + nx * (y + ny * z));
   if (kMode == 0) {
-    float nv = kExact ? (float)((double)*v + alpha * (double)gv) : __fmaf_rn(alphaf, gv, *v);
+    float nv;
+    if (kExact) {
+      if (!bpc::update_cert(*v, gv, alphaf, alphal, &nv)) nv = (float)((double)*v + alpha * (double)gv);
+    } else {
+      nv = __fmaf_rn(alphaf, gv, *v);
+    }
     nv = mac_max(mac_min(gmax, nv), 0.0f);
     *v = nv;
   } else {
@@ -472,10 +496,11 @@ cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njo
   const int float_ok = ((double)(float)halfW == halfW && (double)(float)halfH == halfH && (double)(float)ds == ds);
   if (W >= (1 << 22) || H >= (1 << 22)) return cudaErrorInvalidValue;
   const float wlim = (float)(W - 2), hlim = (float)(H - 2);
+  const float alphal = (float)(alpha - (double)(float)alpha);  // alpha ~ (float)alpha + alphal
 #define WAP_BP(E, M)                                                                                             \
   bp_voxel_kernel<E, M><<<grid, block, 0, st>>>(d_geom, d_jobs, zblocks, dims[0], dims[1], W, H, halfW, halfH, sdd, \
                                                 ds, float_ok, alpha, gmax, (float)halfW, (float)halfH, (float)ds,  \
-                                                (float)alpha, wlim, hlim)
+                                                (float)alpha, alphal, wlim, hlim)
   if (exact) {
     if (mode == 0) WAP_BP(true, 0);
     else WAP_BP(true, 1);
