@@ -161,7 +161,17 @@ WAP_API int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user);
  * TMA-fed fused kernel (grids with nx % 4 == 0, else 2); "pd_zchunk": z
  * planes per block, 0 = autotuned / default; "fp_bricks": 1 (default) = the
  * forward projector reads a 4x4x4 brick-layout copy of each volume, 0 = the
- * linear volume.  One key changes results: the
+ * linear volume.  "bp_ray": 0 (default) = SART backprojects voxel-driven
+ * with the reference's bicubic weights; 1 = SART backprojects with the
+ * matched ray-driven splat (the ray caster's back-projection mode,
+ * SingleScalarVolume.core.h:85-96,149-199, which the reference's
+ * --bp Raybased allocates sums for, TypicalRayProducer.cpp:42-45,100-104)
+ * and updates vol += alpha * contribution / weight where weight > 0, then
+ * clamps to [0, G_Max] (column-sum normalisation); warp-and-project keeps
+ * the voxel-driven backprojection.  "splat_form": 0 (default) = the
+ * ray-driven splat accumulates each slab of a tile's rays in shared memory
+ * and flushes it with float4 atomics; 1 = one global atomic per tap (the
+ * same sums in another order).  One key changes results: the
  * precision form, "flow_bits" = 16 stores the flow solver's dual, flow and
  * linearisation as FP16 pairs during the primal-dual iterations and computes
  * them with fused multiply-adds and hardware reciprocals (FP64 residual sums;
@@ -228,8 +238,11 @@ WAP_API int wap_backproject_voxel(wap_ctx *ctx, int proj, const float *d_corr, c
                                   float *d_vol);
 
 /* Ray-driven matched backprojection: the reference's back-projection mode of
- * the ray caster (SingleScalarVolume.core.h:85-96,149-199), FP32 atomics.
- * d_contrib / d_weight are accumulated into (zero them first). */
+ * the ray caster (SingleScalarVolume.core.h:85-96,149-199): every sample of
+ * the forward projector's march adds corr * w_k and w_k to its 8 trilinear
+ * taps.  Accumulated in shared memory per slab of a tile's rays, flushed with
+ * FP32 atomics (the sums' order varies from run to run).  d_contrib /
+ * d_weight are accumulated into (zero them first). */
 WAP_API int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_contrib, float *d_weight);
 
 /* ---- warp (device pointers) --------------------------------------------- */

@@ -449,6 +449,10 @@ class PSART {
     m_RayProducer->m_ctx = c;
     m_level = -1;
     check(wap_set_tuning(c, "flow_bits", m_flow_bits), c, "flow precision");
+    // --bp Raybased: SART backprojects through the matched ray-driven splat
+    // with column-sum normalisation (the reference only allocates its sums
+    // for this mode, TypicalRayProducer.cpp:42-45,100-104)
+    check(wap_set_tuning(c, "bp_ray", m_RayProducer->m_bp == "Raybased" ? 1 : 0), c, "backprojection mode");
   }
 
   // The whole reconstruction (WaP_Tomo.cpp:473-875); the reference ends the

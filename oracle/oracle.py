@@ -155,6 +155,7 @@ class Oracle:
         _bind(L, "orc_flow_multiscale", _c_int, [_i32, R, R, R, cR, cR, _c_int, _c_int, cR, cR, _c_int, _i32,
                                                  _c_int, R])
         _bind(L, "orc_sart_prox", None, [S, _f64, R, _c_int, _c_int, _c_int, _i32, R, R])
+        _bind(L, "orc_sart_prox_ray", None, [S, _f64, R, _c_int, _c_int, _c_int, _i32, R, R])
         _bind(L, "orc_warp_and_project", None, [S, _f64, R, _c_int, cR, R, R, R])
         _bind(L, "orc_cp_dual", None, [S, _i32, R, R, R, R])
         _bind(L, "orc_cp_primal", None, [S, _i32, _c_int, ctypes.c_void_p, R, R, R, R])
@@ -248,6 +249,13 @@ class Oracle:
         dual = np.zeros((scan.nproj, H, W), self.dt)
         self.lib.orc_sart_prox(ctypes.byref(scan), angles, projs, pstart, pend, nb_sart, np.asarray(box, np.int32),
                                vol, dual)
+        return vol, dual
+
+    def sart_prox_ray(self, scan, angles, projs, pstart, pend, nb_sart, box, vol):
+        W, H = scan.det
+        dual = np.zeros((scan.nproj, H, W), self.dt)
+        self.lib.orc_sart_prox_ray(ctypes.byref(scan), angles, projs, pstart, pend, nb_sart,
+                                   np.asarray(box, np.int32), vol, dual)
         return vol, dual
 
     def warp_and_project(self, scan, angles, projs, proj, rtime, flow_fwd, flow_adj, vol):

@@ -1047,6 +1047,45 @@ void orc_sart_prox(const orc_scan *s, const double *angles, const real *projs, i
   for (size_t i = 0; i < nv; ++i) vol[i] = mac_max(vol[i] * 1.0f, 0.0f);
 }
 
+// The SART proximal operator with the ray-driven matched backprojection
+// (the reference's back-projection mode of the ray caster,
+// SingleScalarVolume.core.h:85-96,149-199, selected by --bp Raybased,
+// TypicalRayProducer.cpp:42-45): the correction is splatted into per-voxel
+// contribution and weight sums, and the volume takes alpha * contribution /
+// weight where the weight is positive (column-sum normalisation), clamped to
+// [0, G_Max], over the box.  The reference never consumes its sums, so this
+// update is the one the library defines for the mode.
+void orc_sart_prox_ray(const orc_scan *s, const double *angles, const real *projs, int pstart, int pend, int nb_sart,
+                       const int box[6], real *vol, real *dual_rows) {
+  const int W = s->det[0], H = s->det[1];
+  const size_t np = (size_t)W * H;
+  const int *d = s->vol;
+  const size_t nv = (size_t)d[0] * d[1] * d[2];
+  std::memset(dual_rows, 0, sizeof(real) * np * s->nproj);
+  std::vector<real> img(np), len(np), wt(np), c(np), contrib(nv), weight(nv);
+  const int num = pend - pstart + 1;
+  const real a = (real)(float)s->alpha, gmax = s->gmax;
+  for (int iter = 1; iter <= nb_sart; ++iter)
+    for (int q = 0; q < num; ++q) {
+      const int pid = (q % 2 == 0) ? pstart + q / 2 : pend - q / 2;
+      orc_forward(s, angles[pid], vol, img.data(), len.data(), wt.data());
+      orc_correction((int)np, projs + np * pid, img.data(), len.data(), dual_rows + np * pid, s->alpha, c.data());
+      std::fill(contrib.begin(), contrib.end(), (real)0);
+      std::fill(weight.begin(), weight.end(), (real)0);
+      orc_ray_backproject(s, angles[pid], c.data(), contrib.data(), weight.data());
+      for (int k = box[4]; k < box[5]; ++k)
+        for (int j = box[2]; j < box[3]; ++j)
+          for (int i = box[0]; i < box[1]; ++i) {
+            const size_t t = i + (size_t)d[0] * (j + (size_t)d[1] * k);
+            const real w = weight[t];
+            if (!(w > (real)0)) continue;
+            real v = vol[t] + a * (contrib[t] / w);
+            vol[t] = v < (real)0 ? (real)0 : (v > gmax ? gmax : v);
+          }
+    }
+  for (size_t i = 0; i < nv; ++i) vol[i] = mac_max(vol[i] * 1.0f, 0.0f);
+}
+
 // WarpAndProjct (WaP_Tomo.cpp:1207-1421) with imROI == 1.
 void orc_warp_and_project(const orc_scan *s, const double *angles, const real *projs, int proj, real rtime,
                           const real *flow_fwd, const real *flow_adj, real *vol) {

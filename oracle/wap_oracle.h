@@ -110,6 +110,11 @@ int orc_flow_multiscale(const int dims[3], const orc_real *I1, const orc_real *I
 /* SART proximal operator on one frame (WaP_Tomo.cpp:1424-1678). */
 void orc_sart_prox(const orc_scan *s, const double *angles, const orc_real *projs, int pstart, int pend, int nb_sart,
                    const int box[6], orc_real *vol, orc_real *dual_rows);
+/* The same with the ray-driven matched backprojection and column-sum
+ * normalisation (--bp Raybased): vol += alpha * contrib / weight where
+ * weight > 0, clamped to [0, G_Max], over the box. */
+void orc_sart_prox_ray(const orc_scan *s, const double *angles, const orc_real *projs, int pstart, int pend,
+                       int nb_sart, const int box[6], orc_real *vol, orc_real *dual_rows);
 
 /* One warp-and-project step (WaP_Tomo.cpp:1207-1421). */
 void orc_warp_and_project(const orc_scan *s, const double *angles, const orc_real *projs, int proj, orc_real rtime,

@@ -151,6 +151,55 @@ def test_ray_backprojection_matches_dead_path(setup, orc):
     assert rel_l2(host(dw), ow) < 1e-5
 
 
+@pytest.mark.parametrize("n,det,nproj", [(48, 64, 12), (61, 80, 12)])
+def test_ray_backprojection_every_angle_and_odd_grids(wapmod, orc, torch_cuda, n, det, nproj):
+    """The shared-memory slab accumulation against the oracle's sequential
+    splat on every projection of a scan (rays of all directions, grazing
+    entries at the silhouette), on a grid whose width is a multiple of 4 (the
+    float4 flush) and one that is not (the scalar flush)."""
+    import oracle as O
+    torch = torch_cuda
+    ang = P.golden_angles(nproj)
+    ctx = wapmod.Context(wapmod.make_scan((n, n, n), (det, det), nproj), ang)
+    try:
+        oscan = O.make_scan((n, n, n), (det, det), nproj)
+        rng = np.random.default_rng(n)
+        for p in range(nproj):
+            corr = rng.normal(size=(det, det)).astype(np.float32)
+            oc, ow = orc.ray_backproject(oscan, ang[p], corr)
+            dcon = torch.zeros((n, n, n), device="cuda")
+            dw = torch.zeros_like(dcon)
+            torch.cuda.synchronize()
+            ctx.backproject_ray(p, dev(torch, corr), dcon, dw)
+            ctx.synchronize()
+            assert rel_l2(host(dw), ow) < 1e-5, "weights, projection %d" % p
+            assert rel_l2(host(dcon), oc) < 1e-5, "contributions, projection %d" % p
+    finally:
+        ctx.close()
+
+
+def test_ray_driven_sart_matches_oracle(setup, orc):
+    """--bp Raybased: the SART proximal operator with the ray-driven matched
+    backprojection and column-sum normalisation, against the oracle's
+    restatement of the same update (within the reordering of the FP32 atomic
+    sums)."""
+    s = setup
+    ctx = s["ctx"]
+    ctx.level_setup(0)
+    _, st, en, _, _ = orc.level_frames(2, NP, 0)
+    v1 = (s["vol"] * 0.5).astype(np.float32)
+    ctx.upload_volume(1, v1)
+    ctx.set_tuning("bp_ray", 1)
+    try:
+        ctx.sart_prox(1, nb_sart=2, cut=8, exact=1)
+    finally:
+        ctx.set_tuning("bp_ray", 0)
+    got = ctx.download_volume(1)
+    ov, _ = orc.sart_prox_ray(s["oscan"], s["ang"], s["projs"], int(st[1]), int(en[1]), 2, [8, N - 8] * 3, v1.copy())
+    assert rel_l2(got, ov) < 1e-5
+    assert not np.array_equal(got, v1)
+
+
 @pytest.mark.parametrize("dt,box", [(0.7, 1), (-1.0, 1), (-1.0, 2)])
 def test_advect_bitexact(setup, orc, dt, box):
     s = setup

@@ -49,7 +49,7 @@ const Opt kOpts[] = {
     {'b', "AlgorithmIter", 1, 1, "algorithm iterations (unused by the live path; default 2)"},
     {'p', "SartIter", 1, 1, "SART nested iterations (default 2)"},
     {0, "prior", 3, 1, "{STV,SAD,ATV} (default ATV)"},
-    {0, "bp", 3, 1, "{Voxelbased,Raybased} (default Voxelbased)"},
+    {0, "bp", 3, 1, "{Voxelbased,Raybased} (default Voxelbased; Raybased: SART backprojects ray-driven)"},
     {'h', "help", 0, 1, "print this help and exit"},
     {0, "version", 0, 1, "print version information and exit"},
     {0, "nproj", 1, 1, "[ext] projections in the stack (default 192, the reference's constant)"},

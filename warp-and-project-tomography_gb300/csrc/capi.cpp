@@ -208,6 +208,10 @@ struct wap_ctx {
   DevMem bricks;          // brick-layout copies of the volumes a projection batch reads
   DevMem jobs_fpb;        // the batch's projection jobs pointing at those copies
   int fp_bricks = 1;      // 1: the forward projector reads brick-layout copies (same bits, faster)
+  int bp_ray = 0;         // 1: SART backprojects ray-driven, normalised by the column sums
+  int splat_direct = 0;   // 1: the ray-driven splat issues a global atomic per tap (comparison form)
+  DevMem ray_acc;         // contributions and weights of a ray-driven SART step (2 V per frame job)
+  DevMem jobs_splat, jobs_rupd;
   std::map<std::pair<int, int>, std::unique_ptr<DevMem[]>> resize_tables;
   DevMem cg_buf;
 
@@ -370,6 +374,29 @@ int sart_frames(wap_ctx *ctx, const std::vector<int> &frames, int nb_sart, const
   TRY(upload(ctx, ctx->jobs_fp, fp));
   TRY(upload(ctx, ctx->jobs_bp, bp));
   int mb[3] = {box[1] - box[0], box[3] - box[2], box[5] - box[4]};
+  // Ray-driven mode: each step's corrections are backprojected by the
+  // matched ray-driven splat into per-job contribution / weight sums, and
+  // the volume takes alpha * contribution / weight (SART's column-sum
+  // normalisation) over the box.
+  const bool ray = ctx->bp_ray != 0;
+  if (ray) {
+    CU(ctx->ray_acc.ensure(sizeof(float) * 2 * ctx->nv * (size_t)std::max(maxn, 1)));
+    std::vector<SplatJob> sj;
+    std::vector<RayUpdJob> uj;
+    for (int s = 0; s < maxnum; ++s)
+      for (int q = step_off[s]; q < step_off[s + 1]; ++q) {
+        float *acc = ctx->ray_acc.as<float>() + (size_t)(q - step_off[s]) * 2 * ctx->nv;
+        sj.push_back(SplatJob{fp[q].corr, fp[q].proj, acc, acc + ctx->nv});
+        RayUpdJob u{};
+        u.vol = bp[q].vol;
+        u.contrib = acc;
+        u.weight = acc + ctx->nv;
+        std::memcpy(u.box, box, sizeof(u.box));
+        uj.push_back(u);
+      }
+    TRY(upload(ctx, ctx->jobs_splat, sj));
+    TRY(upload(ctx, ctx->jobs_rupd, uj));
+  }
   for (int it = 1; it <= nb_sart; ++it)
     for (int s = 0; s < maxnum; ++s) {
       const int n = step_off[s + 1] - step_off[s];
@@ -381,6 +408,14 @@ int sart_frames(wap_ctx *ctx, const std::vector<int> &frames, int nb_sart, const
       ctx->stats.fp_launches++;
       ctx->stats.projections += n;
       ctx->stats.backprojections += n;
+      if (ray) {
+        CU(cudaMemsetAsync(ctx->ray_acc.p, 0, sizeof(float) * 2 * ctx->nv * n, ctx->stream));
+        KL(launch_ray_splat(ctx->geom.as<ProjGeom>(), ctx->jobs_splat.as<SplatJob>() + step_off[s], n, ctx->scan.vol,
+                            W, H, ctx->sd, ctx->stream, ctx->splat_direct != 0));
+        KL(launch_ray_update(ctx->jobs_rupd.as<RayUpdJob>() + step_off[s], n, mb, ctx->scan.vol, ctx->scan.alpha,
+                             ctx->gmax, ctx->stream));
+        continue;
+      }
       KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_bp.as<BpJob>() + step_off[s], n, mb, ctx->scan.vol, W, H,
                          ctx->halfW, ctx->halfH, (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha, ctx->gmax, 0,
                          exact, ctx->stream));
@@ -1260,6 +1295,14 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
     CHECK(value == 0 || value == 1, WAP_EINVAL, "fp_bricks must be 0 or 1");
     ctx->fp_bricks = value;
     return WAP_OK;
+  } else if (k == "splat_form") {
+    CHECK(value == 0 || value == 1, WAP_EINVAL, "splat_form must be 0 or 1");
+    ctx->splat_direct = value;
+    return WAP_OK;
+  } else if (k == "bp_ray") {
+    CHECK(value == 0 || value == 1, WAP_EINVAL, "bp_ray must be 0 or 1");
+    ctx->bp_ray = value;
+    return WAP_OK;
   } else if (k == "pd_zchunk") {
     CHECK(value >= 0, WAP_EINVAL, "pd_zchunk must be >= 0");
     ctx->pd_zchunk = value;
@@ -1508,7 +1551,7 @@ int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_co
   std::vector<SplatJob> jobs{SplatJob{d_corr, proj, d_contrib, d_weight}};
   TRY(upload(ctx, ctx->jobs_misc, jobs));
   KL(launch_ray_splat(ctx->geom.as<ProjGeom>(), ctx->jobs_misc.as<SplatJob>(), 1, ctx->scan.vol, ctx->scan.det[0],
-                      ctx->scan.det[1], ctx->sd, ctx->stream));
+                      ctx->scan.det[1], ctx->sd, ctx->stream, ctx->splat_direct != 0));
   return WAP_OK;
 }
 

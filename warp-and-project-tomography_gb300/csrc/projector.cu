@@ -310,6 +310,283 @@ __global__ void __launch_bounds__(128) splat_kernel(const ProjGeom *__restrict__
   cast_ray(smp, n, vz, vu, tn, tf, sd);
 }
 
+// ---------------------------------------------------------------------------
+// Ray-driven matched backprojection with shared-memory accumulation
+// (SingleScalarVolume.core.h:85-96,149-199: every forward-projection sample
+// adds corr * w_k and w_k to its 8 trilinear taps).  A block's 128 rays (a
+// 16 x 8 pixel tile) are nearly parallel, so at any distance t along them
+// their samples lie in a small region.  The block marches its rays together
+// through slabs of t (kSlab voxels deep): each slab's taps are first bounded
+// (a pass over the slab's sample positions alone), then accumulated into a
+// shared-memory window of that bounding box with shared atomics, and the
+// window is flushed to the global sums with float4 atomic adds, one per
+// aligned group of four voxels that received anything.  Taps outside the
+// window's capacity go to global atomics directly, so any geometry is
+// handled.  The sample sequence is the forward projector's, replayed by a
+// resumable copy of cast_ray (same float operations in the same order).
+// ---------------------------------------------------------------------------
+namespace rbp {
+constexpr int kCap = 4096;       // window cells (contributions + weights: 32 KB)
+constexpr float kSlab = 6.0f;    // slab depth in t (voxel units)
+constexpr int kThreads = 128;
+
+// cast_ray as a generator: settle() advances to the next pending sample (or
+// the end), peek() is that sample's t, take() returns its position.
+struct March {
+  float vz[3], vu[3], step[3], tnear, tfar, sd, t1, tb, t, p[3], tMax[3], tDelta[3];
+  int mode;  // 0: first sample pending, 1: in a segment, 2: between segments, 3: done
+  __device__ __forceinline__ void init(const int n[3], const float z[4], const float u[4], float tn, float tf,
+                                       float s) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      vz[a] = z[a];
+      vu[a] = u[a];
+      step[a] = u[a] * s;
+    }
+    tnear = tn;
+    tfar = tf;
+    sd = s;
+    t1 = tn;
+    const float pos1[3] = {vz[0] + vu[0] * t1, vz[1] + vu[1] * t1, vz[2] + vu[2] * t1};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      p[a] = pos1[a];
+      const int bs = n[a];
+      tDelta[a] = 0.0f;
+      if (vu[a] == 0.0f) {
+        tMax[a] = tfar;
+      } else if (vu[a] < 0.0f) {
+        const int blk = ((int)ceilf(pos1[a] - 0.5f) - 1) / bs;
+        tMax[a] = ((float)(blk * bs) + 0.5f - vz[a]) / vu[a];
+        tDelta[a] = (float)(-(1 * bs)) / vu[a];
+      } else {
+        const int blk = ((int)floorf(pos1[a] - 0.5f)) / bs;
+        tMax[a] = ((float)((blk + 1) * bs) + 0.5f - vz[a]) / vu[a];
+        tDelta[a] = (float)(1 * bs) / vu[a];
+      }
+    }
+    mode = 0;
+  }
+  __device__ __forceinline__ void settle() {
+    for (;;) {
+      if (mode == 0 || mode == 3) return;
+      if (mode == 1) {
+        if (t < tb) return;
+        if (tMax[0] < tMax[1]) {
+          if (tMax[0] < tMax[2]) tMax[0] += tDelta[0];
+          else tMax[2] += tDelta[2];
+        } else {
+          if (tMax[1] < tMax[2]) tMax[1] += tDelta[1];
+          else tMax[2] += tDelta[2];
+        }
+        t1 = tb;
+        mode = 2;
+      }
+      if (!(t1 < tfar)) {
+        mode = 3;
+        return;
+      }
+      tb = mac_min(mac_min(tMax[0], tMax[1]), tMax[2]);
+      if (tb > tfar) tb = tfar;
+      t = ceilf((t1 - tnear) / sd) * sd + tnear;
+      p[0] = vz[0] + vu[0] * t;
+      p[1] = vz[1] + vu[1] * t;
+      p[2] = vz[2] + vu[2] * t;
+      mode = 1;
+    }
+  }
+  __device__ __forceinline__ float peek() const { return mode == 0 ? tnear : mode == 1 ? t : INFINITY; }
+  // the pending sample's position, then advance (call with peek() finite)
+  __device__ __forceinline__ void take(float &x, float &y, float &z) {
+    x = p[0];
+    y = p[1];
+    z = p[2];
+    if (mode == 0) {
+      mode = 2;
+    } else {
+      t += sd;
+      p[0] += step[0];
+      p[1] += step[1];
+      p[2] += step[2];
+    }
+    settle();
+  }
+};
+
+// The sampler's clamp-then-truncate cell of a position.
+__device__ __forceinline__ void cell(float x, float y, float z, const int n[3], int &i, int &j, int &k, float &t0,
+                                    float &t1, float &t2) {
+  x = mac_max(mac_min(x, (float)(n[0] - 1)), 0.0f);
+  y = mac_max(mac_min(y, (float)(n[1] - 1)), 0.0f);
+  z = mac_max(mac_min(z, (float)(n[2] - 1)), 0.0f);
+  i = (int)x;
+  j = (int)y;
+  k = (int)z;
+  t0 = x - (float)i;
+  t1 = y - (float)j;
+  t2 = z - (float)k;
+}
+}  // namespace rbp
+
+__global__ void __launch_bounds__(rbp::kThreads) bp_ray_kernel(const ProjGeom *__restrict__ geom,
+                                                               const SplatJob *__restrict__ jobs, int nx, int ny,
+                                                               int nz, int W, int H, float sd) {
+  using namespace rbp;
+  __shared__ __align__(16) float win_c[kCap];
+  __shared__ __align__(16) float win_w[kCap];
+  __shared__ int bb[6];
+  __shared__ unsigned tstart;
+  const int tid = threadIdx.x;
+  int pi, pj;
+  tile_pixel(pi, pj);
+  const SplatJob job = jobs[blockIdx.z];
+  const int n[3] = {nx, ny, nz};
+  March m;
+  m.mode = 3;
+  float corr = 0.0f;
+  if (pi < W && pj < H) {
+    const ProjGeom &g = geom[job.proj];
+    float vz[4], vu[4], tn, tf;
+    produce_ray(g, nx, ny, nz, (float)pi, (float)pj, vz, vu, tn, tf);
+    if (tn < tf) {
+      m.init(n, vz, vu, tn, tf, sd);
+      corr = __ldg(job.corr + pi + pj * W);
+    }
+  }
+  for (int q = tid; q < kCap; q += kThreads) {
+    win_c[q] = 0.0f;
+    win_w[q] = 0.0f;
+  }
+  if (tid == 0) tstart = 0x7f800000u;  // +inf; t >= 0 so float order = bit order
+  __syncthreads();
+  if (m.mode != 3) atomicMin(&tstart, __float_as_uint(m.peek()));
+  __syncthreads();
+  if (tstart == 0x7f800000u) return;  // no ray of this tile meets the volume
+  float T = __uint_as_float(tstart);
+  const bool vec = (nx & 3) == 0 && ((reinterpret_cast<uintptr_t>(job.contrib) | reinterpret_cast<uintptr_t>(job.weight)) & 15) == 0;
+  for (;;) {
+    const float Tlo = T;
+    T += kSlab;
+    if (tid < 3) bb[tid] = 0x7fffffff;
+    else if (tid < 6) bb[tid] = -1;
+    __syncthreads();
+    // the slab's cells: the ray segment t in [max(Tlo, next sample), min(T,
+    // tfar)] bounds the sample positions up to the float recurrence's drift
+    // (hundredths of a voxel); one cell of margin on each side covers it and
+    // taps, and any tap outside the window still goes to a global atomic
+    {
+      int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-1, -1, -1};
+      const float tn = m.peek();
+      if (tn < T) {
+        const float ta = fmaxf(Tlo, tn), tb = fminf(T, m.tfar);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float pa = m.vz[a] + m.vu[a] * ta, pb = m.vz[a] + m.vu[a] * tb;
+          const float mn = mac_max(mac_min(fminf(pa, pb), (float)(n[a] - 1)), 0.0f);
+          const float mx = mac_max(mac_min(fmaxf(pa, pb), (float)(n[a] - 1)), 0.0f);
+          lo[a] = max((int)mn - 1, 0);
+          hi[a] = min((int)mx + 2, n[a] - 1);
+        }
+      }
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        for (int o = 16; o > 0; o >>= 1) {
+          lo[a] = min(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+          hi[a] = max(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+      }
+      if ((tid & 31) == 0 && hi[0] >= 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          atomicMin(&bb[a], lo[a]);
+          atomicMax(&bb[3 + a], hi[a]);
+        }
+      }
+    }
+    __syncthreads();
+    const bool any = bb[3] >= 0;
+    // the window: x from a multiple of 4 (aligned float4 flushes), clipped to kCap cells
+    const int ox = bb[0] & ~3, oy = bb[1], oz = bb[2];
+    const int wx = any ? ((bb[3] - ox + 1) + 3) & ~3 : 4;
+    const int wy = any ? min(bb[4] - oy + 1, max(1, kCap / wx)) : 1;
+    const int wz = any ? min(bb[5] - oz + 1, max(1, kCap / (wx * wy))) : 1;
+    const bool fits = wx * wy <= kCap;
+    // pass 2: accumulate
+    while (m.peek() < T) {
+      float x, y, z, t0, t1, t2;
+      int ci, cj, ck;
+      m.take(x, y, z);
+      cell(x, y, z, n, ci, cj, ck, t0, t1, t2);
+      const float M0 = 1.0f - t0, M1 = 1.0f - t1, M2 = 1.0f - t2;
+      const float w[8] = {M0 * M1 * M2, t0 * M1 * M2, M0 * t1 * M2, t0 * t1 * M2,
+                          M0 * M1 * t2, t0 * M1 * t2, M0 * t1 * t2, t0 * t1 * t2};
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int x2 = ci + (c & 1), y2 = cj + ((c >> 1) & 1), z2 = ck + ((c >> 2) & 1);
+        if (x2 >= nx || y2 >= ny || z2 >= nz) continue;
+        const int lx = x2 - ox, ly = y2 - oy, lz = z2 - oz;
+        const float cw = corr * w[c];
+        if (fits && (unsigned)lx < (unsigned)wx && (unsigned)ly < (unsigned)wy && (unsigned)lz < (unsigned)wz) {
+          const int q = lx + wx * (ly + wy * lz);
+          atomicAdd(win_c + q, cw);
+          atomicAdd(win_w + q, w[c]);
+        } else {
+          const size_t id = (size_t)x2 + (size_t)nx * (y2 + (size_t)ny * z2);
+          atomicAdd(job.contrib + id, cw);
+          atomicAdd(job.weight + id, w[c]);
+        }
+      }
+    }
+    __syncthreads();
+    // flush: aligned groups of 4 cells along x that received anything
+    if (any && fits) {
+      const int gx = wx >> 2, ngroups = gx * wy * wz;
+      for (int q = tid; q < ngroups; q += kThreads) {
+        const int qx = q % gx, qy = (q / gx) % wy, qz = q / (gx * wy);
+        const int base = 4 * qx + wx * (qy + wy * qz);
+        const float4 c4 = *reinterpret_cast<const float4 *>(win_c + base);
+        const float4 w4 = *reinterpret_cast<const float4 *>(win_w + base);
+        if (w4.x == 0.0f && w4.y == 0.0f && w4.z == 0.0f && w4.w == 0.0f && c4.x == 0.0f && c4.y == 0.0f &&
+            c4.z == 0.0f && c4.w == 0.0f)
+          continue;
+        *reinterpret_cast<float4 *>(win_c + base) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        *reinterpret_cast<float4 *>(win_w + base) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const int x = ox + 4 * qx, y = oy + qy, z = oz + qz;
+        const size_t id = (size_t)x + (size_t)nx * (y + (size_t)ny * z);
+        if (vec && x + 3 < nx) {
+          atomicAdd(reinterpret_cast<float4 *>(job.contrib + id), c4);
+          atomicAdd(reinterpret_cast<float4 *>(job.weight + id), w4);
+        } else {
+          const float cs[4] = {c4.x, c4.y, c4.z, c4.w}, ws[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            if (x + e < nx && (ws[e] != 0.0f || cs[e] != 0.0f)) {
+              atomicAdd(job.contrib + id + e, cs[e]);
+              atomicAdd(job.weight + id + e, ws[e]);
+            }
+        }
+      }
+    }
+    if (!__syncthreads_or(m.peek() < INFINITY)) break;
+  }
+}
+
+__global__ void ray_update_kernel(const RayUpdJob *__restrict__ jobs, int zblocks, int nx, int ny, float alpha,
+                                  float gmax) {
+  const int jb = blockIdx.z / zblocks;
+  const RayUpdJob job = jobs[jb];
+  const int x = job.box[0] + blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = job.box[2] + blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = job.box[4] + (blockIdx.z % zblocks) * blockDim.z + threadIdx.z;
+  if (x >= job.box[1] || y >= job.box[3] || z >= job.box[5]) return;
+  const size_t t = (size_t)x + (size_t)nx * (y + (size_t)ny * z);
+  const float w = job.weight[t];
+  if (!(w > 0.0f)) return;
+  float v = job.vol[t] + alpha * (job.contrib[t] / w);
+  v = v < 0.0f ? 0.0f : (v > gmax ? gmax : v);
+  job.vol[t] = v;
+}
+
 __global__ void correction_kernel(int n, const float *__restrict__ meas, const float *__restrict__ img,
                                   const float *__restrict__ len, float *dual, double alpha, float *corr) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -471,11 +748,23 @@ cudaError_t launch_brick(const float *vol, float *out, const int dims[3], cudaSt
   return cudaGetLastError();
 }
 
+cudaError_t launch_ray_update(const RayUpdJob *d_jobs, int njobs, const int maxbox[3], const int dims[3],
+                              double alpha, float gmax, cudaStream_t st) {
+  if (njobs <= 0 || maxbox[0] <= 0 || maxbox[1] <= 0 || maxbox[2] <= 0) return cudaSuccess;
+  const dim3 block(32, 4, 2);
+  const int zblocks = (maxbox[2] + 1) / 2;
+  if ((long long)zblocks * njobs > 65535) return cudaErrorInvalidValue;
+  const dim3 grid((maxbox[0] + 31) / 32, (maxbox[1] + 3) / 4, zblocks * njobs);
+  ray_update_kernel<<<grid, block, 0, st>>>(d_jobs, zblocks, dims[0], dims[1], (float)alpha, gmax);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ray_splat(const ProjGeom *d_geom, const SplatJob *d_jobs, int njobs, const int dims[3], int W,
-                             int H, float sd, cudaStream_t st) {
+                             int H, float sd, cudaStream_t st, bool direct) {
   if (njobs <= 0) return cudaSuccess;
   dim3 grid((W + 15) / 16, (H + 7) / 8, njobs);
-  splat_kernel<<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd);
+  if (direct) splat_kernel<<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd);
+  else bp_ray_kernel<<<grid, rbp::kThreads, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd);
   return cudaGetLastError();
 }
 

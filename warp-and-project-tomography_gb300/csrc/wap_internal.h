@@ -88,8 +88,20 @@ cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const 
 cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njobs, int maxbox[3], const int dims[3],
                             int W, int H, double halfW, double halfH, float sdd, double ds, double alpha, float gmax,
                             int mode, int exact, cudaStream_t st);
+// direct: every tap a global atomic (the plain form); otherwise the
+// shared-memory slab accumulation of bp_ray_kernel.
 cudaError_t launch_ray_splat(const ProjGeom *d_geom, const SplatJob *d_jobs, int njobs, const int dims[3], int W,
-                             int H, float sd, cudaStream_t st);
+                             int H, float sd, cudaStream_t st, bool direct = false);
+// The ray-driven SART update over a job's box: where weight > 0,
+// vol = clamp(vol + alpha * (contrib / weight), 0, gmax) in float.
+struct RayUpdJob {
+  float *vol;
+  const float *contrib;
+  const float *weight;
+  int box[6];
+};
+cudaError_t launch_ray_update(const RayUpdJob *d_jobs, int njobs, const int maxbox[3], const int dims[3],
+                              double alpha, float gmax, cudaStream_t st);
 cudaError_t launch_correction(int n, const float *meas, const float *img, const float *len, float *dual,
                               double alpha, float *corr, cudaStream_t st);
 

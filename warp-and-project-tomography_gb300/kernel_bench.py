@@ -2,7 +2,7 @@
 CUDA-event timing on the library's stream).
 
     python kernel_bench.py --kernel pd --n 256 --iters 100 [--pd-form 0|1|2|3]
-    python kernel_bench.py --kernel fp|bp|bp_exact|advect|all --n 256 --det 384
+    python kernel_bench.py --kernel fp|bp|bp_exact|bp_ray|advect|all --n 256 --det 384
 
 Prints one JSON line per kernel: milliseconds per launch and the achieved
 bandwidth against the kernel's algorithmic bytes:
@@ -11,6 +11,9 @@ bandwidth against the kernel's algorithmic bytes:
   fp      forward projection, V*4 + 16*D bytes (volume once, 4 outputs per pixel)
   bp      voxel-driven backprojection over the ROI, 2*V*4 + 4*D bytes
   advect  one warp of a 1-channel volume by a 3-channel flow, V*(2+3)*4 bytes
+  bp_ray  ray-driven matched backprojection (contribution and weight sums,
+          read and written once each: 16*V + 4*D bytes), --splat-form 1 for the
+          one-global-atomic-per-tap form
 Used to make the per-kernel ncu captures summarised under profiles/.
 """
 import argparse
@@ -31,7 +34,7 @@ def main():
     import build
     import wap
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", default="all", choices=["pd", "fp", "bp", "bp_exact", "advect", "all"])
+    ap.add_argument("--kernel", default="all", choices=["pd", "fp", "bp", "bp_exact", "bp_ray", "advect", "all"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--det", type=int, default=384)
     ap.add_argument("--iters", type=int, default=20)
@@ -39,6 +42,7 @@ def main():
     ap.add_argument("--pd-form", type=int, default=0, help="0 autotuned, 1 fused, 2 primal+dual, 3 TMA-fed fused")
     ap.add_argument("--pd-zchunk", type=int, default=0)
     ap.add_argument("--flow-bits", type=int, default=32, help="16: the precision form (FP16 flow state)")
+    ap.add_argument("--splat-form", type=int, default=0, help="1: one global atomic per tap in the ray-driven splat")
     ap.add_argument("--fp-bricks", type=int, default=1, help="0: the projector reads the linear volume (1: brick-layout copy)")
     a = ap.parse_args()
     build.build()
@@ -96,6 +100,13 @@ def main():
         for exact in ([1] if a.kernel == "bp_exact" else [0] if a.kernel == "bp" else [0, 1]):
             ms = timed(lambda: ctx.backproject_voxel(3, corr, box, 0, exact, v2), a.reps)
             report("bp_exact" if exact else "bp", ms, 2 * nb * 4 + 4 * d * d)
+    if a.kernel in ("bp_ray", "all"):
+        ctx.set_tuning("splat_form", a.splat_form)
+        corr = torch.rand((d, d), device="cuda", generator=g) - 0.5
+        con = torch.zeros((n, n, n), device="cuda")
+        wsum = torch.zeros_like(con)
+        ms = timed(lambda: ctx.backproject_ray(3, corr, con, wsum), a.reps)
+        report("bp_ray", ms, 16 * nv + 4 * d * d, {"splat_form": a.splat_form})
     if a.kernel in ("advect", "all"):
         flow = torch.randn((3, n, n, n), device="cuda", generator=g) * 2
         out = torch.zeros((1, n, n, n), device="cuda")
