@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cctype>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -548,16 +549,29 @@ class PSART {
     return sc;
   }
 
+  // CImg's load dispatches on the extension (CImg.h:46142-46290): .tif/.tiff
+  // through libtiff, Analyze/NIfTI otherwise.
+  static bool is_tiff(const char *path) {
+    const std::string p(path);
+    const size_t dot = p.rfind('.');
+    std::string ext = dot == std::string::npos ? "" : p.substr(dot + 1);
+    for (char &c : ext) c = (char)std::tolower((unsigned char)c);
+    return ext == "tif" || ext == "tiff";
+  }
+
   void load_projections(const char *path) {
     int dims[4], type = 0;
-    check(wap_analyze_info(path, dims, &type), nullptr, "PSART: projection stack");
+    const bool tiff = is_tiff(path);
+    check(tiff ? wap_tiff_info(path, dims, nullptr, nullptr) : wap_analyze_info(path, dims, &type), nullptr,
+          "PSART: projection stack");
     const int W = dims[0], H = dims[1], D = dims[2];
     if (W != m_sd.det[0] || H != m_sd.det[1])
       throw Error(WAP_EINVAL, "PSART: projection images are " + std::to_string(W) + "x" + std::to_string(H) +
                                   ", the command line says " + std::to_string(m_sd.det[0]) + "x" +
                                   std::to_string(m_sd.det[1]));
     std::vector<float> stack((size_t)W * H * D * dims[3]);
-    check(wap_analyze_load(path, stack.data(), stack.size()), nullptr, "PSART: projection stack");
+    check(tiff ? wap_tiff_load(path, stack.data(), stack.size()) : wap_analyze_load(path, stack.data(), stack.size()),
+          nullptr, "PSART: projection stack");
     const int P = m_sd.nproj;
     std::vector<int> first(P), count(P);
     check(wap_split_z(D, P, first.data(), count.data()), nullptr, "PSART: split of the projection stack");

@@ -3,7 +3,7 @@
  *
  * These are the inputs and outputs around the reference's hot path: the
  * projection stack and result volumes in Analyze 7.5 / NIfTI-1 as CImg reads
- * and writes them, the projection-angle text file PSART's constructor reads,
+ * and writes them, TIFF projection stacks as CImg's libtiff loader reads them, the projection-angle text file PSART's constructor reads,
  * the z-split of a projection stack into per-projection images, and the
  * low-discrepancy angle generator of the reference's sampling scripts.
  * Every call returns WAP_OK or a WAP_E* status (wap.h).
@@ -38,6 +38,19 @@ WAP_API int wap_analyze_load(const char *path, float *h_out, size_t count);
  * (name.img), or one 352-byte-header file for a .nii name; a name without an
  * extension gets .hdr/.img.  voxel_size may be NULL (spacing 1). */
 WAP_API int wap_analyze_save(const char *path, const float *h_data, const int *dims4, const float *voxel_size);
+
+/* A TIFF projection stack as CImg<float>::load_tiff reads it (CImg.h:47445-
+ * 47700; the reference enables libtiff for its projection input,
+ * WaP_Tomo.h:7-8): every page is one z slice, each sample cast to float with
+ * no scaling.  dims4 = W, H, pages, samples per pixel; bits and
+ * sample_format (1 unsigned, 2 signed, 3 IEEE) of the first page (any may be
+ * NULL).  Read: classic little- or big-endian TIFF, strips or tiles, one
+ * sample per pixel of 8/16/32/64 bits, no compression, PackBits, LZW or
+ * Deflate (through the system's zlib), horizontal-differencing predictor;
+ * anything else, and any malformed file, is WAP_EIO. */
+WAP_API int wap_tiff_info(const char *path, int *dims4, int *bits, int *sample_format);
+/* Loads all pages, page after page (x fastest), into h_out (count >= W*H*pages floats). */
+WAP_API int wap_tiff_load(const char *path, float *h_out, size_t count);
 
 /* Reads up to n whitespace-separated angles (degrees) the way PSART's
  * constructor does (WaP_Tomo.cpp:324-331, `stream >> inputdegree[i]`):

@@ -41,7 +41,7 @@ const Opt kOpts[] = {
     {'u', "imgUV", 1, 2, "projection width and height"},
     {'c', "voxelspacing", 2, 1, "voxel spacing (default 1)"},
     {'d', "detector spacing", 2, 1, "detector spacing (default 1)"},
-    {'i', "projsvolume", 3, 20, "projection stack (.hdr/.img Analyze or .nii)"},
+    {'i', "projsvolume", 3, 20, "projection stack (.hdr/.img Analyze, .nii or .tif/.tiff)"},
     {'j', "sdd", 2, 1, "source to detector distance (default 200)"},
     {'g', "sid", 2, 1, "source to iso-centre distance (default 400)"},
     {0, "oxyz", 2, 3, "volume centre offset x y z (default 0)"},

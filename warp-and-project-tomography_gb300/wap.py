@@ -162,6 +162,8 @@ SIGNATURES = {
     "wap_server_now": (_c_double, [_vp]),
     "wap_server_memory": (_c_int, [_vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     # include/wap/wap_io.h
+    "wap_tiff_info": (_c_int, [ctypes.c_char_p, _vp, _vp, _vp]),
+    "wap_tiff_load": (_c_int, [ctypes.c_char_p, _vp, ctypes.c_size_t]),
     "wap_analyze_info": (_c_int, [ctypes.c_char_p, _vp, _vp]),
     "wap_analyze_load": (_c_int, [ctypes.c_char_p, _vp, ctypes.c_size_t]),
     "wap_analyze_save": (_c_int, [ctypes.c_char_p, _vp, _vp, _vp]),
@@ -462,6 +464,26 @@ def level_frames(scan, level):
 
 def _path(p):
     return os.fsencode(p)
+
+
+def tiff_info(path):
+    """(W, H, pages, samples per pixel), bits, sample format of a TIFF stack."""
+    d = np.zeros(4, np.int32)
+    b, f = ctypes.c_int(0), ctypes.c_int(0)
+    r = load().wap_tiff_info(_path(path), d.ctypes.data, ctypes.addressof(b), ctypes.addressof(f))
+    if r != WAP_OK:
+        raise WapError("wap_tiff_info(%s) failed with status %d" % (path, r))
+    return tuple(int(x) for x in d), b.value, f.value
+
+
+def tiff_load(path):
+    """A TIFF stack as float32 (pages, H, W), as CImg<float>::load_tiff reads it."""
+    (w, h, p, c), _, _ = tiff_info(path)
+    out = np.zeros((p, h, w), np.float32)
+    r = load().wap_tiff_load(_path(path), out.ctypes.data, out.size)
+    if r != WAP_OK:
+        raise WapError("wap_tiff_load(%s) failed with status %d" % (path, r))
+    return out
 
 
 def analyze_info(path):
