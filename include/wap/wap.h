@@ -294,6 +294,17 @@ WAP_API int wap_sart_prox(wap_ctx *ctx, int frame, int nb_sart, int cut, int exa
 /* PSART::WarpAndProjct (WaP_Tomo.cpp:1207-1421) for one projection. */
 WAP_API int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exact);
 
+/* PSART::AdaptiveWarp (WaP_Tomo.cpp:878-1204; commented out in the reference)
+ * on one frame of the current level: nb_warp sweeps over the frame's window
+ * in order, each projection forward-projecting the volume warped by
+ * flow[max(0, frame-1)] (correction against one dual row, zeroed per call),
+ * backprojecting into a delta volume that accumulates over the sweep (ROI box
+ * from cut), and adding alpha * the delta warped back by flow[max(0, frame-2)]
+ * then clamping to [0, G_Max]; max(vol, 0) at the end.  The reference's
+ * per-projection time (m_ProjIndex[i].rElapsed) is never set; the warp-and-
+ * project step's clamp((i - fTime) / tunit, -1, 1) is used. */
+WAP_API int wap_adaptive_warp(wap_ctx *ctx, int frame, int nb_warp, int cut, int exact);
+
 /* One outer iteration of PSART::Render at the current level
  * (WaP_Tomo.cpp:514-827): CP prior + SART over all frames, flow for every
  * adjacent pair, warp-and-project over the schedule's frames. */

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "wap/wap.h"
+#include "wap/coherent_volume.hpp"
 #include "wap/wap_io.h"
 
 namespace wap19 {
@@ -742,6 +743,7 @@ inline void GenerateImage_GetCorrections(TypicalRayProducer *rp) {
 }  // namespace wap19
 
 #ifdef WAP19_GLOBAL_NAMES
+using wap19::CoherentVolume;
 using wap19::PSART;
 using wap19::VolumeData;
 using wap19::Frame_item;

@@ -156,6 +156,7 @@ class Oracle:
                                                  _c_int, R])
         _bind(L, "orc_sart_prox", None, [S, _f64, R, _c_int, _c_int, _c_int, _i32, R, R])
         _bind(L, "orc_sart_prox_ray", None, [S, _f64, R, _c_int, _c_int, _c_int, _i32, R, R])
+        _bind(L, "orc_adaptive_warp", None, [S, _f64, R, _c_int, _c_int, cR, cR, _c_int, _i32, R, R, R])
         _bind(L, "orc_warp_and_project", None, [S, _f64, R, _c_int, cR, R, R, R])
         _bind(L, "orc_cp_dual", None, [S, _i32, R, R, R, R])
         _bind(L, "orc_cp_primal", None, [S, _i32, _c_int, ctypes.c_void_p, R, R, R, R])
@@ -257,6 +258,11 @@ class Oracle:
         self.lib.orc_sart_prox_ray(ctypes.byref(scan), angles, projs, pstart, pend, nb_sart,
                                    np.asarray(box, np.int32), vol, dual)
         return vol, dual
+
+    def adaptive_warp(self, scan, angles, projs, pstart, pend, ftime, tunit, nb_warp, box, flow_fwd, flow_adj, vol):
+        self.lib.orc_adaptive_warp(ctypes.byref(scan), angles, projs, pstart, pend, ftime, tunit, nb_warp,
+                                   np.asarray(box, np.int32), flow_fwd, flow_adj, vol)
+        return vol
 
     def warp_and_project(self, scan, angles, projs, proj, rtime, flow_fwd, flow_adj, vol):
         self.lib.orc_warp_and_project(ctypes.byref(scan), angles, projs, proj, rtime, flow_fwd, flow_adj, vol)

@@ -509,3 +509,23 @@ int wref_split_z(int depth, int nb, int *first, int *count) {
   return (int)L.size();
 }
 }
+
+extern "C" {
+// The reference's CoherentVolume (CoherentVolume.cpp:33-258) on a volume of
+// one block per axis (the case its byte-scaled pointer steps leave defined):
+// every GetValue, the block range from GetMinMaxValue.
+int wref_coherent_volume(const int bs[3], const int dims[3], float *data, float *values, double *minmax) {
+  CoherentVolume cv(bs[0], bs[1], bs[2]);
+  cv.SetDimensions(dims);
+  int bn[3];
+  cv.GetBlockNum(bn);
+  if (bn[0] != 1 || bn[1] != 1 || bn[2] != 1) return -1;
+  cv.AllocateBlocks();
+  cv.SetData(data);
+  for (int z = 0; z < dims[2]; ++z)
+    for (int y = 0; y < dims[1]; ++y)
+      for (int x = 0; x < dims[0]; ++x) values[x + dims[0] * (y + dims[1] * z)] = cv.GetValue(x, y, z);
+  cv.GetMinMaxValue(minmax[0], minmax[1]);
+  return 0;
+}
+}

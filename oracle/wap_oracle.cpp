@@ -1110,6 +1110,39 @@ void orc_warp_and_project(const orc_scan *s, const double *angles, const real *p
   }
 }
 
+// PSART::AdaptiveWarp (WaP_Tomo.cpp:878-1204, commented out in the
+// reference), with the per-projection time the reference never fills
+// (m_ProjIndex[i].rElapsed) taken as clamp((i - ftime) / tunit, -1, 1).
+void orc_adaptive_warp(const orc_scan *s, const double *angles, const real *projs, int pstart, int pend, real ftime,
+                       real tunit, int nb_warp, const int box[6], const real *flow_fwd, const real *flow_adj,
+                       real *vol) {
+  const int W = s->det[0], H = s->det[1];
+  const size_t np = (size_t)W * H;
+  const int *d = s->vol;
+  const size_t nv = (size_t)d[0] * d[1] * d[2];
+  const real aabb[6] = {0, (real)d[0], 0, (real)d[1], 0, (real)d[2]};
+  std::vector<real> warped(nv), img(np), len(np), wt(np), c(np), delta(nv), back(nv), dual(np, 0.0f);
+  const double alpha = s->alpha;
+  const real gmax = s->gmax;
+  for (int iter = 1; iter <= nb_warp; ++iter) {
+    std::fill(delta.begin(), delta.end(), (real)0);  // deltaVol.fill(0.0f) (:911)
+    for (int i = pstart; i <= pend; ++i) {
+      real td = (i - ftime) / tunit;
+      td = mac_min(mac_max(-1.0f, td), 1.0f);
+      orc_advect(d, aabb, flow_fwd, vol, 1, td, warped.data(), s->threads);
+      orc_forward(s, angles[i], warped.data(), img.data(), len.data(), wt.data());
+      orc_correction((int)np, projs + np * i, img.data(), len.data(), dual.data(), s->alpha, c.data());
+      orc_bp_voxel(s, angles[i], c.data(), box, 1, delta.data());
+      orc_advect(d, aabb, flow_adj, delta.data(), 1, -td, back.data(), s->threads);
+      for (size_t t = 0; t < nv; ++t) {
+        const real x = (real)((double)vol[t] + (double)back[t] * alpha);
+        vol[t] = (x < 0.0f) ? 0.0f : ((x > gmax) ? gmax : x);  // cut(0.0, G_Max) (:1161)
+      }
+    }
+  }
+  for (size_t t = 0; t < nv; ++t) vol[t] = mac_max(vol[t] * 1.0f, 0.0f);
+}
+
 // CP dual for frame f (WaP_Tomo.cpp:586-619).
 void orc_cp_dual(const orc_scan *s, const int box[6], const real *xbar_f, const real *xbar_next, real *ytv_f,
                  real *ytp_f) {

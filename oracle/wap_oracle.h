@@ -110,6 +110,11 @@ int orc_flow_multiscale(const int dims[3], const orc_real *I1, const orc_real *I
 /* SART proximal operator on one frame (WaP_Tomo.cpp:1424-1678). */
 void orc_sart_prox(const orc_scan *s, const double *angles, const orc_real *projs, int pstart, int pend, int nb_sart,
                    const int box[6], orc_real *vol, orc_real *dual_rows);
+/* PSART::AdaptiveWarp (WaP_Tomo.cpp:878-1204, commented out in the reference)
+ * on one frame: window [pstart, pend], frame time ftime, time unit tunit. */
+void orc_adaptive_warp(const orc_scan *s, const double *angles, const orc_real *projs, int pstart, int pend,
+                       orc_real ftime, orc_real tunit, int nb_warp, const int box[6], const orc_real *flow_fwd,
+                       const orc_real *flow_adj, orc_real *vol);
 /* The same with the ray-driven matched backprojection and column-sum
  * normalisation (--bp Raybased): vol += alpha * contrib / weight where
  * weight > 0, clamped to [0, G_Max], over the box. */

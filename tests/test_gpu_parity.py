@@ -360,6 +360,29 @@ def test_warp_and_project_bitexact(setup, orc):
         assert np.array_equal(ctx.download_volume(1), cur)
 
 
+def test_adaptive_warp_bitexact(setup, orc):
+    """AdaptiveWarp (the reference's commented-out per-frame warp sweep,
+    WaP_Tomo.cpp:878-1204) on frame 2 with two sweeps, against the oracle."""
+    s = setup
+    ctx = s["ctx"]
+    F = ctx.level_setup(1)  # the second time level: 4 frames
+    assert F >= 3
+    _, st, en, ft, tu = orc.level_frames(2, NP, 1)
+    f = 2
+    v = (s["vol"] * 0.6).astype(np.float32)
+    fl1 = (s["flow"] * 0.5).astype(np.float32)
+    fl0 = (s["flow"] * -0.4).astype(np.float32)
+    ctx.upload_volume(f, v)
+    ctx.upload_flow(f - 1, fl1)
+    ctx.upload_flow(f - 2, fl0)
+    ctx.adaptive_warp(f, nb_warp=2, cut=8, exact=1)
+    want = orc.adaptive_warp(s["oscan"], s["ang"], s["projs"], int(st[f]), int(en[f]), float(ft[f]), float(tu), 2,
+                             [8, N - 8] * 3, fl1, fl0, v.copy())
+    got = ctx.download_volume(f)
+    assert np.array_equal(got, want)
+    assert not np.array_equal(got, v)
+
+
 def test_outer_iteration_bitexact(setup, orc, wapmod):
     s = setup
     ctx, O = s["ctx"], s["O"]

@@ -195,13 +195,15 @@ __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__
 
 // vol += alpha * adv (double, CImg operator* / operator+=), cut(0, G_Max),
 // then max(vol * imROI, 0) with imROI == 1 (WaP_Tomo.cpp:1378-1412).
+// FLOOR = false: the cut alone (AdaptiveWarp, WaP_Tomo.cpp:1160-1161, floors once at its end).
+template <bool FLOOR>
 __global__ void wap_accumulate_kernel(size_t n, float *__restrict__ vol, const float *__restrict__ adv, double alpha,
                                       float gmax) {
   const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   float x = (float)((double)vol[i] + (double)adv[i] * alpha);
   x = (x < 0.0f) ? 0.0f : ((x > gmax) ? gmax : x);
-  vol[i] = mac_max(x * 1.0f, 0.0f);
+  vol[i] = FLOOR ? mac_max(x * 1.0f, 0.0f) : x;
 }
 
 __global__ void wap_accumulate_batch_kernel(const AccJob *__restrict__ jobs, size_t n, double alpha, float gmax) {
@@ -260,8 +262,10 @@ cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d
   return cudaSuccess;
 }
 
-cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st) {
-  wap_accumulate_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, vol, adv, alpha, gmax);
+cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st,
+                                  bool floor) {
+  if (floor) wap_accumulate_kernel<true><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, vol, adv, alpha, gmax);
+  else wap_accumulate_kernel<false><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, vol, adv, alpha, gmax);
   return cudaGetLastError();
 }
 

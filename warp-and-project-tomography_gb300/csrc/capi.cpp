@@ -518,6 +518,80 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
   return WAP_OK;
 }
 
+// PSART::AdaptiveWarp (WaP_Tomo.cpp:878-1204, commented out in the
+// reference): per sweep, a zeroed delta volume; then for each projection of
+// the frame's window in order, the forward projection of the volume warped by
+// flow[max(0, f-1)] with the correction against one dual row (zeroed once per
+// call), the bicubic backprojection added into the delta over the ROI box, and
+// vol = cut(vol + alpha * warp(delta by flow[max(0, f-2)], -rtime), 0, G_Max);
+// the delta keeps accumulating over the window.  At the end max(vol * imROI,
+// 0).  rtime is the warp-and-project step's clamp((i - fTime) / tunit, -1, 1):
+// the reference reads m_ProjIndex[i].rElapsed, a list it never fills.
+int adaptive_warp(wap_ctx *ctx, int f, int nb_warp, int cut, int exact) {
+  TRY(ensure_world(ctx));
+  int box[6];
+  TRY(roi_box(ctx, cut, box));
+  const size_t nv = ctx->nv, np = ctx->np;
+  const int W = ctx->scan.det[0], H = ctx->scan.det[1];
+  const int *d = ctx->scan.vol;
+  const float aabb[6] = {0, (float)d[0], 0, (float)d[1], 0, (float)d[2]};
+  const int ff = std::max(0, f - 1), fa = std::max(0, f - 2);
+  float *vol = vol_ptr(ctx, f);
+  float *warped = ctx->warped.as<float>() + (size_t)f * nv, *delta = ctx->delta.as<float>() + (size_t)f * nv,
+        *back = ctx->back.as<float>() + (size_t)f * nv;
+  float *dual = ctx->dual.as<float>() + (size_t)f * ctx->maxwin * np, *corr = ctx->corr.as<float>() + (size_t)f * np;
+  const int n = ctx->en[f] - ctx->st[f] + 1;
+  std::vector<AdvectJob> adv;
+  std::vector<FpJob> fp;
+  std::vector<BpJob> bp;
+  for (int i = ctx->st[f]; i <= ctx->en[f]; ++i) {
+    float td = (i - ctx->ft[f]) / ctx->tunit;
+    td = mac_min(mac_max(-1.0f, td), 1.0f);
+    adv.push_back(AdvectJob{flow_ptr(ctx, ff), vol, warped, td});
+    adv.push_back(AdvectJob{flow_ptr(ctx, fa), delta, back, -td});
+    FpJob j{};
+    j.vol = warped;
+    j.proj = i;
+    j.meas = ctx->projs;
+    j.dual = dual;
+    j.corr = corr;
+    fp.push_back(j);
+    BpJob b{};
+    b.vol = delta;
+    b.corr = corr;
+    b.proj = i;
+    std::memcpy(b.box, box, sizeof(box));
+    bp.push_back(b);
+  }
+  TRY(upload(ctx, ctx->jobs_adv, adv));
+  TRY(upload(ctx, ctx->jobs_fp, fp));
+  TRY(upload(ctx, ctx->jobs_bp, bp));
+  int mb[3] = {box[1] - box[0], box[3] - box[2], box[5] - box[4]};
+  const bool fast = ctx->flow_bits == 16;
+  CU(cudaMemsetAsync(dual, 0, sizeof(float) * np, ctx->stream));
+  for (int it = 1; it <= nb_warp; ++it) {
+    CU(cudaMemsetAsync(delta, 0, sizeof(float) * nv, ctx->stream));
+    for (int q = 0; q < n; ++q) {
+      KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + 2 * q, 1, 1, ctx->stream,
+                       fast));
+      KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_fp.as<FpJob>() + q, 1, d, W, H, ctx->sd, ctx->scan.alpha,
+                        ctx->stream, false));
+      KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_bp.as<BpJob>() + q, 1, mb, d, W, H, ctx->halfW,
+                         ctx->halfH, (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha, ctx->gmax, 1, exact,
+                         ctx->stream));
+      KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + 2 * q + 1, 1, 1, ctx->stream,
+                       fast));
+      KL(launch_wap_accumulate(nv, vol, back, ctx->scan.alpha, ctx->gmax, ctx->stream, false));
+      ctx->stats.fp_launches++;
+      ctx->stats.projections++;
+      ctx->stats.backprojections++;
+      ctx->stats.advect_voxels += 2.0 * (double)nv;
+    }
+  }
+  KL(launch_roi_floor(nv, vol, ctx->stream));
+  return WAP_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Flow
 // ---------------------------------------------------------------------------
@@ -1640,6 +1714,17 @@ int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exa
   TRY(wap_step(ctx, items, exact));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
+}
+
+int wap_adaptive_warp(wap_ctx *ctx, int frame, int nb_warp, int cut, int exact) {
+  CHECK(ctx, WAP_EINVAL, "null argument");
+  CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
+  CHECK(ctx->level >= 0, WAP_ESTATE, "no level set up");
+  CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
+  CHECK(frame >= 0 && frame < ctx->F && nb_warp >= 0, WAP_EINVAL, "frame or sweep count out of range");
+  CHECK(cut >= 0 && 2 * cut < ctx->scan.vol[0] && 2 * cut < ctx->scan.vol[1] && 2 * cut < ctx->scan.vol[2], WAP_EINVAL,
+        "cut must leave a non-empty ROI");
+  return adaptive_warp(ctx, frame, nb_warp, cut, exact);
 }
 
 int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1, wap_stats *stats) {

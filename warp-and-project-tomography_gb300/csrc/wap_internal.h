@@ -117,8 +117,10 @@ void world_table(const int dims[3], const float aabb[6], float *h);
 // tolerance); false: the reference's arithmetic, bit for bit.
 cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d_world, const AdvectJob *d_jobs,
                           int njobs, int nc, cudaStream_t st, bool fast = false);
-// vol = clamp_cut(vol + alpha*adv) then max(vol*roi, 0) (WaP_Tomo.cpp:1378-1412).
-cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st);
+// vol = clamp_cut(vol + alpha*adv) then max(vol*roi, 0) (WaP_Tomo.cpp:1378-1412);
+// floor = false leaves out the max(., 0).
+cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st,
+                                  bool floor = true);
 cudaError_t launch_roi_floor(size_t n, float *vol, cudaStream_t st);
 struct AccJob {
   float *vol;

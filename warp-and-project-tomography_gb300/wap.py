@@ -142,6 +142,7 @@ SIGNATURES = {
                                           _c_int, _c_float, _c_float, _c_int, _vp, _vp, _vp]),
     "wap_sart_prox": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int]),
     "wap_warp_and_project": (_c_int, [_vp, _c_int, _c_int, _c_float, _c_int]),
+    "wap_adaptive_warp": (_c_int, [_vp, _c_int, _c_int, _c_int, _c_int]),
     "wap_outer_iteration": (_c_int, [_vp, ctypes.POINTER(Schedule), ctypes.POINTER(Stats)]),
     "wap_outer_iteration_frames": (_c_int, [_vp, ctypes.POINTER(Schedule), _c_int, _c_int, ctypes.POINTER(Stats)]),
     "wap_outer_iteration_nsteps": (_c_int, [_vp, ctypes.POINTER(Schedule)]),
@@ -412,6 +413,9 @@ class Context:
 
     def warp_and_project(self, frame, proj, rtime, exact=1):
         self.call("wap_warp_and_project", frame, proj, rtime, exact)
+
+    def adaptive_warp(self, frame, nb_warp=1, cut=8, exact=1):
+        self.call("wap_adaptive_warp", frame, nb_warp, cut, exact)
 
     def outer_iteration(self, sched):
         st = Stats()
