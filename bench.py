@@ -82,8 +82,10 @@ def parse():
                     help="32: the reference's arithmetic; 16: the precision form (FP16 flow state)")
     ap.add_argument("--precision-steps", type=int, default=2,
                     help="frame-steps re-timed in the precision form for the line's precision_form object (0: skip)")
-    ap.add_argument("--batch-jobs", type=int, default=12,
+    ap.add_argument("--batch-jobs", type=int, default=48,
                     help="scans of the batched-form comparison added to the line (0: skip)")
+    ap.add_argument("--batch-flow-iters", type=int, default=40,
+                    help="primal-dual iterations per level and warp of the batched scans' flows")
     ap.add_argument("--kernel-reps", type=int, default=5,
                     help="timed launches per kernel of the line's per-kernel roofline table (0: skip)")
     ap.add_argument("--full-outer", action="store_true",
@@ -532,10 +534,10 @@ def run_gb300(args):
         result["serving"], result["serving_precision"] = serving.run(
             wap, torch, n_jobs=args.serve_jobs, rate=args.serve_rate, workers=args.serve_workers, flow_bits=(32, 16))
     if rank == 0 and world == 1 and args.batch_jobs > 0:
-        # Batched form: uneven scans looped through the plain path vs overlapped
-        # through the request loop (same results, checked).
+        # Batched form: uneven scans looped through the plain path vs reconstructed
+        # together through wap_batch (same results, checked).
         import serving
-        result["batched"] = serving.run_batched(wap, torch, n_jobs=args.batch_jobs)
+        result["batched"] = serving.run_batched(wap, torch, n_jobs=args.batch_jobs, flow_iters=args.batch_flow_iters)
     if rank == 0:
         print(json.dumps(result))
     if dist:

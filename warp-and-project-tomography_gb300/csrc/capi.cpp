@@ -1848,3 +1848,401 @@ int wap_outer_iteration(wap_ctx *ctx, const wap_schedule *sch, wap_stats *stats)
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Batched form (wap_batch.h): the scans' SART steps merged into work-queue
+// launches, the CP iteration captured as a CUDA graph, flows and warp-and-
+// project overlapped on the scans' streams.
+// ===========================================================================
+#include <thread>
+
+#include "wap/wap_batch.h"
+
+struct wap_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<wap_ctx *> ctxs;
+  int fp_shape = -1, bp_shape = -1;  // -1: autotune on the next outer iteration
+  DevMem qfp, qbp, qbrick, counter, bricks;
+  std::string err;
+};
+
+namespace {
+
+int bfail(wap_batch *b, int code, const std::string &msg) {
+  if (b) b->err = msg;
+  return code;
+}
+#define BCU(expr)                                                                                    \
+  do {                                                                                               \
+    cudaError_t _e = (expr);                                                                         \
+    if (_e != cudaSuccess) return bfail(b, WAP_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+// The merged SART sweep of one CP iteration: per step the brick copies, the
+// projections and the backprojections of every frame of every scan whose
+// window has that step, each one work-queue launch.
+struct BatchPlan {
+  std::vector<QFpJob> fp;
+  std::vector<QBpJob> bp;
+  std::vector<QBrickJob> br;
+  std::vector<int> off;  // step s: jobs [off[s], off[s+1]) in fp / bp / br
+  std::vector<int> fp_items, bp_items, br_items;
+  int nb_sart = 0, exact = 1;
+};
+
+// dry: the tuning form of the jobs (projection images into the correction
+// slots with no correction or dual update, backprojection into the delta
+// volumes), which changes no state of the scans.
+int batch_plan(wap_batch *b, const wap_schedule *sch, BatchPlan &P, bool dry) {
+  P = BatchPlan();
+  P.nb_sart = sch[0].nb_sart;
+  P.exact = sch[0].bp_exact;
+  int maxnum = 0;
+  std::vector<std::vector<std::vector<int>>> orders(b->ctxs.size());
+  for (size_t c = 0; c < b->ctxs.size(); ++c) {
+    wap_ctx *x = b->ctxs[c];
+    orders[c].resize(x->F);
+    for (int f = 0; f < x->F; ++f) {
+      sart_order(x->st[f], x->en[f], orders[c][f]);
+      maxnum = std::max(maxnum, (int)orders[c][f].size());
+    }
+  }
+  size_t max_slot = 0;
+  std::vector<size_t> slot_of;  // brick-copy offset (floats) of each job
+  for (int s = 0; s < maxnum; ++s) {
+    P.off.push_back((int)P.fp.size());
+    size_t slot = 0;
+    for (size_t c = 0; c < b->ctxs.size(); ++c) {
+      wap_ctx *x = b->ctxs[c];
+      int box[6];
+      roi_box(x, sch[c].cut, box);
+      const size_t bf = brick_floats(x->scan.vol);
+      for (int f = 0; f < x->F; ++f) {
+        if (s >= (int)orders[c][f].size()) continue;
+        const int pid = orders[c][f][s];
+        QFpJob q{};
+        q.job.proj = pid;
+        q.job.corr = x->corr.as<float>() + (size_t)f * x->np;
+        if (dry) {
+          q.job.img = q.job.corr;
+        } else {
+          q.job.meas = x->projs;
+          q.job.dual = x->dual.as<float>() + ((size_t)f * x->maxwin + (pid - x->st[f])) * x->np;
+        }
+        q.geom = x->geom.as<ProjGeom>();
+        for (int a = 0; a < 3; ++a) q.n[a] = x->scan.vol[a];
+        q.W = x->scan.det[0];
+        q.H = x->scan.det[1];
+        q.sd = x->sd;
+        q.alpha = x->scan.alpha;
+        q.bricked = 1;
+        QBrickJob r{};
+        r.vol = vol_ptr(x, f);
+        for (int a = 0; a < 3; ++a) r.n[a] = x->scan.vol[a];
+        slot_of.push_back(slot);
+        slot += bf;
+        QBpJob p{};
+        p.job.vol = dry ? x->delta.as<float>() + (size_t)f * x->nv : vol_ptr(x, f);
+        p.job.corr = q.job.corr;
+        p.job.proj = pid;
+        std::memcpy(p.job.box, box, sizeof(box));
+        p.geom = q.geom;
+        p.P = make_bp_params(x->scan.vol, q.W, q.H, x->halfW, x->halfH, (float)x->scan.sdd, x->scan.ds,
+                             x->scan.alpha, x->gmax);
+        P.fp.push_back(q);
+        P.bp.push_back(p);
+        P.br.push_back(r);
+      }
+    }
+    max_slot = std::max(max_slot, slot);
+  }
+  P.off.push_back((int)P.fp.size());
+  BCU(b->bricks.ensure(sizeof(float) * std::max<size_t>(max_slot, 1)));
+  for (size_t j = 0; j < P.br.size(); ++j) {
+    P.br[j].out = b->bricks.as<float>() + slot_of[j];
+    P.fp[j].job.vol = P.br[j].out;
+  }
+  const int nsteps = (int)P.off.size() - 1;
+  for (int s = 0; s < nsteps; ++s) {
+    const int o = P.off[s], n = P.off[s + 1] - o;
+    P.fp_items.push_back(fp_queue_items(P.fp.data() + o, n, std::max(b->fp_shape, 0)));
+    P.bp_items.push_back(bp_queue_items(P.bp.data() + o, n, std::max(b->bp_shape, 0)));
+    P.br_items.push_back(brick_queue_items(P.br.data() + o, n));
+  }
+  return WAP_OK;
+}
+
+int batch_upload(wap_batch *b, const BatchPlan &P) {
+  BCU(b->qfp.ensure(sizeof(QFpJob) * std::max<size_t>(P.fp.size(), 1)));
+  BCU(b->qbp.ensure(sizeof(QBpJob) * std::max<size_t>(P.bp.size(), 1)));
+  BCU(b->qbrick.ensure(sizeof(QBrickJob) * std::max<size_t>(P.br.size(), 1)));
+  BCU(b->counter.ensure(sizeof(int) * 4));
+  if (!P.fp.empty()) {
+    BCU(cudaMemcpyAsync(b->qfp.p, P.fp.data(), sizeof(QFpJob) * P.fp.size(), cudaMemcpyHostToDevice, b->stream));
+    BCU(cudaMemcpyAsync(b->qbp.p, P.bp.data(), sizeof(QBpJob) * P.bp.size(), cudaMemcpyHostToDevice, b->stream));
+    BCU(cudaMemcpyAsync(b->qbrick.p, P.br.data(), sizeof(QBrickJob) * P.br.size(), cudaMemcpyHostToDevice,
+                        b->stream));
+  }
+  BCU(cudaStreamSynchronize(b->stream));
+  return WAP_OK;
+}
+
+// The launches of one step (brick copies, projections, backprojections).
+int batch_step(wap_batch *b, const BatchPlan &P, int s, int mode) {
+  const int o = P.off[s], n = P.off[s + 1] - o;
+  int *ctr = b->counter.as<int>();
+  BCU(launch_brick_queue(b->qbrick.as<QBrickJob>() + o, n, P.br_items[s], ctr, b->stream));
+  BCU(launch_fp_queue(b->qfp.as<QFpJob>() + o, n, P.fp_items[s], ctr + 1, std::max(b->fp_shape, 0), b->stream));
+  BCU(launch_bp_queue(b->qbp.as<QBpJob>() + o, n, P.bp_items[s], ctr + 2, std::max(b->bp_shape, 0), P.exact, mode,
+                      b->stream));
+  return WAP_OK;
+}
+
+// Tile shapes by timing every shape on the batch's largest step, on the dry
+// form of its jobs.
+int batch_autotune(wap_batch *b, const wap_schedule *sch) {
+  if (b->fp_shape >= 0 && b->bp_shape >= 0) return WAP_OK;
+  const int keep_fp = b->fp_shape, keep_bp = b->bp_shape;
+  BatchPlan P;
+  int best_step = 0, pick_fp = 0, pick_bp = 0;
+  float best_fp = 1e30f, best_bp = 1e30f;
+  cudaEvent_t e0, e1;
+  BCU(cudaEventCreate(&e0));
+  BCU(cudaEventCreate(&e1));
+  int rc = WAP_OK;
+  for (int shape = 0; shape < std::max(kFpShapes, kBpShapes) && rc == WAP_OK; ++shape) {
+    b->fp_shape = std::min(shape, kFpShapes - 1);
+    b->bp_shape = std::min(shape, kBpShapes - 1);
+    rc = batch_plan(b, sch, P, true);
+    if (rc == WAP_OK) rc = batch_upload(b, P);
+    if (rc != WAP_OK || P.fp.empty()) break;
+    if (shape == 0)
+      for (size_t s = 0; s + 1 < P.off.size(); ++s)
+        if (P.off[s + 1] - P.off[s] > P.off[best_step + 1] - P.off[best_step]) best_step = (int)s;
+    const int o = P.off[best_step], n = P.off[best_step + 1] - o;
+    int *ctr = b->counter.as<int>();
+    cudaError_t e = launch_brick_queue(b->qbrick.as<QBrickJob>() + o, n, P.br_items[best_step], ctr, b->stream);
+    float ms[2] = {0.0f, 0.0f};
+    for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
+      auto go = [&]() {
+        return kind == 0 ? launch_fp_queue(b->qfp.as<QFpJob>() + o, n, P.fp_items[best_step], ctr + 1, b->fp_shape,
+                                           b->stream)
+                         : launch_bp_queue(b->qbp.as<QBpJob>() + o, n, P.bp_items[best_step], ctr + 2, b->bp_shape,
+                                           P.exact, 1, b->stream);
+      };
+      e = go();  // warm-up
+      if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+      for (int r = 0; r < 3 && e == cudaSuccess; ++r) e = go();
+      if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[kind], e0, e1);
+    }
+    if (e != cudaSuccess) {
+      rc = bfail(b, WAP_ECUDA, std::string("batch tuning: ") + cudaGetErrorString(e));
+      break;
+    }
+    if (shape < kFpShapes && ms[0] < best_fp) best_fp = ms[0], pick_fp = shape;
+    if (shape < kBpShapes && ms[1] < best_bp) best_bp = ms[1], pick_bp = shape;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->fp_shape = keep_fp >= 0 ? keep_fp : pick_fp;
+  b->bp_shape = keep_bp >= 0 ? keep_bp : pick_bp;
+  return rc;
+}
+
+CpArgs batch_cp_args(wap_ctx *ctx, const int box[6]) {
+  CpArgs ca;
+  for (int a = 0; a < 3; ++a) ca.n[a] = ctx->scan.vol[a];
+  std::memcpy(ca.box, box, sizeof(ca.box));
+  ca.f0 = 0;
+  ca.F = ctx->F;
+  ca.Ftot = ctx->F;
+  ca.sigma = (float)(.9 / (8.0f * 1.0f));
+  ca.tau = 1.0f;
+  ca.tv_w = (float)ctx->scan.tv_w;
+  ca.tp_w = (float)ctx->scan.tp_w;
+  ca.gmax = ctx->gmax;
+  return ca;
+}
+
+// One CP iteration over every scan (WaP_Tomo.cpp:563-690): per scan the CP
+// dual and primal, then the merged SART sweeps, then per scan the SART floor
+// and the over-relaxation.  Stream work only, so it can be captured.
+int batch_cp_iteration(wap_batch *b, const wap_schedule *sch, const BatchPlan &P) {
+  for (size_t c = 0; c < b->ctxs.size(); ++c) {
+    wap_ctx *ctx = b->ctxs[c];
+    int box[6];
+    roi_box(ctx, sch[c].cut, box);
+    const CpArgs ca = batch_cp_args(ctx, box);
+    BCU(launch_cp_dual(ca, ctx->xbar.as<float>(), ctx->zero_vol.as<float>(), ctx->ytv.as<float>(),
+                       ctx->ytp.as<float>(), b->stream));
+    BCU(launch_cp_primal(ca, ctx->ytp.as<float>(), ctx->ytv.as<float>(), ctx->vols.as<float>(),
+                         ctx->xprev.as<float>(), b->stream));
+    BCU(cudaMemsetAsync(ctx->dual.p, 0, sizeof(float) * ctx->F * ctx->maxwin * ctx->np, b->stream));
+  }
+  const int nsteps = (int)P.off.size() - 1;
+  for (int it = 1; it <= P.nb_sart; ++it)
+    for (int s = 0; s < nsteps; ++s) TRY(batch_step(b, P, s, 0));
+  for (size_t c = 0; c < b->ctxs.size(); ++c) {
+    wap_ctx *ctx = b->ctxs[c];
+    int box[6];
+    roi_box(ctx, sch[c].cut, box);
+    const CpArgs ca = batch_cp_args(ctx, box);
+    BCU(launch_roi_floor(ctx->nv * ctx->F, ctx->vols.as<float>(), b->stream));
+    BCU(launch_cp_overrelax(ca, ctx->vols.as<float>(), ctx->xprev.as<float>(), ctx->xbar.as<float>(), b->stream));
+  }
+  return WAP_OK;
+}
+
+// stream `dst` waits for the work enqueued on `src` so far
+cudaError_t stream_follow(cudaStream_t dst, cudaStream_t src) {
+  cudaEvent_t ev;
+  cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
+  e = cudaEventRecord(ev, src);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(dst, ev, 0);
+  cudaEventDestroy(ev);
+  return e;
+}
+
+}  // namespace
+
+extern "C" {
+
+int wap_batch_create(wap_batch **out, wap_ctx *const *ctxs, int n) {
+  if (!out || !ctxs || n < 1) return WAP_EINVAL;
+  *out = nullptr;
+  std::unique_ptr<wap_batch> b(new wap_batch);
+  for (int i = 0; i < n; ++i) {
+    wap_ctx *x = ctxs[i];
+    if (!x || !has_scan(x) || x->level < 0 || !x->projs) return WAP_ESTATE;
+    if (x->device != ctxs[0]->device) return WAP_EINVAL;
+    for (int j = 0; j < i; ++j)
+      if (ctxs[j] == x) return WAP_EINVAL;
+    b->ctxs.push_back(x);
+  }
+  b->device = ctxs[0]->device;
+  if (cudaSetDevice(b->device) != cudaSuccess) return WAP_ENODEV;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return WAP_ECUDA;
+  *out = b.release();
+  return WAP_OK;
+}
+
+void wap_batch_destroy(wap_batch *b) {
+  if (!b) return;
+  if (b->stream) {
+    cudaStreamSynchronize(b->stream);
+    cudaStreamDestroy(b->stream);
+  }
+  delete b;
+}
+
+const char *wap_batch_last_error(const wap_batch *b) { return b ? b->err.c_str() : "null batch"; }
+
+int wap_batch_set_tuning(wap_batch *b, int fp_shape, int bp_shape) {
+  if (!b || fp_shape < -1 || fp_shape >= kFpShapes || bp_shape < -1 || bp_shape >= kBpShapes) return WAP_EINVAL;
+  b->fp_shape = fp_shape;
+  b->bp_shape = bp_shape;
+  return WAP_OK;
+}
+
+int wap_batch_get_tuning(const wap_batch *b, int *h_fp_shape, int *h_bp_shape) {
+  if (!b || !h_fp_shape || !h_bp_shape) return WAP_EINVAL;
+  *h_fp_shape = b->fp_shape;
+  *h_bp_shape = b->bp_shape;
+  return WAP_OK;
+}
+
+int wap_batch_outer_iteration(wap_batch *b, const wap_schedule *scheds, wap_stats *stats) {
+  if (!b || !scheds) return WAP_EINVAL;
+  const int n = (int)b->ctxs.size();
+  for (int c = 0; c < n; ++c) {
+    const int rc = check_schedule(b->ctxs[c], &scheds[c], 0, b->ctxs[c]->F);
+    if (rc != WAP_OK) return bfail(b, rc, "scan " + std::to_string(c) + ": " + b->ctxs[c]->err);
+    if (scheds[c].nb_sart != scheds[0].nb_sart || scheds[c].bp_exact != scheds[0].bp_exact ||
+        scheds[c].n_cp != scheds[0].n_cp)
+      return bfail(b, WAP_EINVAL, "the scans of a batch share n_cp, nb_sart and bp_exact");
+  }
+  BCU(cudaSetDevice(b->device));
+  for (wap_ctx *x : b->ctxs) {
+    x->stats = wap_stats{};
+    BCU(stream_follow(b->stream, x->stream));  // the batch follows each scan's earlier work
+  }
+  cudaEvent_t t0, t1;
+  BCU(cudaEventCreate(&t0));
+  BCU(cudaEventCreate(&t1));
+  BCU(cudaEventRecord(t0, b->stream));
+  // (1) CP + SART: tune, plan, capture one CP iteration as a graph, replay it
+  warm_queue_kernels();
+  TRY(batch_autotune(b, scheds));
+  BatchPlan P;
+  TRY(batch_plan(b, scheds, P, false));
+  TRY(batch_upload(b, P));
+  if (scheds[0].n_cp > 0) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = batch_cp_iteration(b, scheds, P);
+    const cudaError_t ec = cudaStreamEndCapture(b->stream, &graph);
+    if (rc != WAP_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    BCU(ec);
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    BCU(ei);
+    int rcl = WAP_OK;
+    for (int icp = 1; icp <= scheds[0].n_cp && rcl == WAP_OK; ++icp)
+      if (cudaGraphLaunch(exec, b->stream) != cudaSuccess) rcl = bfail(b, WAP_ECUDA, "cudaGraphLaunch failed");
+    cudaGraphExecDestroy(exec);
+    if (rcl != WAP_OK) return rcl;
+  }
+  // (2) flows and (3) warp-and-project per scan, concurrently on their streams
+  std::vector<int> rcs(n, WAP_OK);
+  for (wap_ctx *x : b->ctxs) BCU(stream_follow(x->stream, b->stream));
+  std::vector<std::thread> th;
+  for (int c = 0; c < n; ++c)
+    th.emplace_back([&, c]() {
+      wap_ctx *ctx = b->ctxs[c];
+      int rc = cudaSetDevice(b->device) == cudaSuccess ? WAP_OK : WAP_ECUDA;
+      for (int f = 0; rc == WAP_OK && f + 1 < ctx->F; ++f) rc = flow_pair(ctx, &scheds[c], f);
+      if (rc == WAP_OK) rc = wap_pass(ctx, &scheds[c], 0, ctx->F);
+      rcs[c] = rc;
+    });
+  for (auto &t : th) t.join();
+  for (int c = 0; c < n; ++c)
+    if (rcs[c] != WAP_OK) return bfail(b, rcs[c], "scan " + std::to_string(c) + ": " + b->ctxs[c]->err);
+  for (wap_ctx *x : b->ctxs) BCU(stream_follow(b->stream, x->stream));
+  BCU(cudaEventRecord(t1, b->stream));
+  BCU(cudaEventSynchronize(t1));
+  float ms = 0.0f;
+  BCU(cudaEventElapsedTime(&ms, t0, t1));
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  if (stats) {
+    wap_stats s{};
+    for (wap_ctx *x : b->ctxs) {
+      s.flow_pd_iterations += x->stats.flow_pd_iterations;
+      s.kernel_launches += x->stats.kernel_launches;
+      s.pd_voxel_iters += x->stats.pd_voxel_iters;
+      s.advect_voxels += x->stats.advect_voxels;
+      s.projections += x->stats.projections;
+      s.backprojections += x->stats.backprojections;
+      s.ms_flow += x->stats.ms_flow;
+      s.ms_wap += x->stats.ms_wap;
+      s.cp_frame_passes += (long long)scheds[0].n_cp * x->F;
+    }
+    const int nsteps = (int)P.off.size() - 1;
+    s.kernel_launches += (long long)scheds[0].n_cp * (3LL * nsteps * P.nb_sart + 4LL * n);
+    s.projections += (long long)scheds[0].n_cp * P.nb_sart * (long long)P.fp.size();
+    s.backprojections += (long long)scheds[0].n_cp * P.nb_sart * (long long)P.bp.size();
+    s.ms_cp = ms;
+    *stats = s;
+  }
+  return WAP_OK;
+}
+
+}  // extern "C"

@@ -10,6 +10,7 @@
 // the sample counts) are a sequential recurrence that must be replayed, not
 // reformulated.  Each warp owns an 8x4 pixel patch so the warp's 32 rays stay
 // within a few voxels of each other and the trilinear gathers hit L1.
+#include <algorithm>
 #include <cstring>
 #include <type_traits>
 
@@ -257,13 +258,12 @@ __device__ __forceinline__ void tile_pixel(int &i, int &j) {
   j = blockIdx.y * 8 + (w >> 1) * 4 + (lane >> 3);
 }
 
+// One detector pixel (i, j) of a projection job: the ray, its march, the
+// outputs and the fused correction.  Shared by the per-launch and the
+// work-queue forms, so both compute the same bits.
 template <class View>
-__global__ void __launch_bounds__(128) fp_kernel(const ProjGeom *__restrict__ geom, const FpJob *__restrict__ jobs,
-                                                 int nx, int ny, int nz, int W, int H, float sd, double alpha) {
-  int i, j;
-  tile_pixel(i, j);
-  if (i >= W || j >= H) return;
-  const FpJob job = jobs[blockIdx.z];
+__device__ __forceinline__ void fp_pixel(const ProjGeom *__restrict__ geom, const FpJob &job, int nx, int ny, int nz,
+                                         int W, int H, float sd, double alpha, int i, int j) {
   const ProjGeom &g = geom[job.proj];
   const int n[3] = {nx, ny, nz};
   float vz[4], vu[4], tn, tf;
@@ -292,6 +292,16 @@ __global__ void __launch_bounds__(128) fp_kernel(const ProjGeom *__restrict__ ge
     job.corr[k] = c;
     if (job.dual) job.dual[k] = (float)((double)y + alpha * (double)c);
   }
+}
+
+template <class View>
+__global__ void __launch_bounds__(128) fp_kernel(const ProjGeom *__restrict__ geom, const FpJob *__restrict__ jobs,
+                                                 int nx, int ny, int nz, int W, int H, float sd, double alpha) {
+  int i, j;
+  tile_pixel(i, j);
+  if (i >= W || j >= H) return;
+  const FpJob job = jobs[blockIdx.z];
+  fp_pixel<View>(geom, job, nx, ny, nz, W, H, sd, alpha, i, j);
 }
 
 __global__ void __launch_bounds__(128) splat_kernel(const ProjGeom *__restrict__ geom,
@@ -633,43 +643,46 @@ __device__ __forceinline__ float small_floor(float v) {
 }
 __device__ __forceinline__ int small_f2i(float fl) { return __float_as_int(fl + 8388608.0f) - 0x4B000000; }
 
-// The host passes the scalars in both precisions (halfWf/halfHf/dsf/alphaf
-// are the float roundings); float_ok says halfW, halfH and ds are exact
-// floats, so that a single double operation rounded to float equals the
-// float operation.  The pixel test px < 2 || px >= W-2 on px = (int)_px is
-// the same as !(2 <= _px < W-2) for every float _px (NaN included), and for
-// _px inside that range (int)_px = floor(_px).
+// Scalars of a voxel-driven backprojection: the host passes halfW, halfH, ds
+// and alpha in both precisions (the f suffixes are the float roundings;
+// alphal = alpha - (float)alpha); float_ok says halfW, halfH and ds are exact
+// floats, so that a single double operation rounded to float equals the float
+// operation.
+struct BpParams {
+  int nx, ny, W, H;
+  double halfW, halfH;
+  float sdd;
+  double ds;
+  int float_ok;
+  double alpha;
+  float gmax, halfWf, halfHf, dsf, alphaf, alphal, wlim, hlim;
+};
+
+// One voxel (x, y, z) of a backprojection job.  The pixel test px < 2 || px >=
+// W-2 on px = (int)_px is the same as !(2 <= _px < W-2) for every float _px
+// (NaN included), and for _px inside that range (int)_px = floor(_px).
 template <bool kExact, int kMode>
-__global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restrict__ geom,
-                                                       const BpJob *__restrict__ jobs, int zblocks, int nx, int ny,
-                                                       int W, int H, double halfW, double halfH, float sdd,
-                                                       double ds, int float_ok, double alpha, float gmax,
-                                                       float halfWf, float halfHf, float dsf, float alphaf,
-                                                       float alphal, float wlim, float hlim) {
-  const int jb = blockIdx.z / zblocks;
-  const BpJob job = jobs[jb];
-  const int x = job.box[0] + blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = job.box[2] + blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = job.box[4] + (blockIdx.z % zblocks) * blockDim.z + threadIdx.z;
-  if (x >= job.box[1] || y >= job.box[3] || z >= job.box[5]) return;
+__device__ __forceinline__ void bp_voxel(const ProjGeom *__restrict__ geom, const BpParams &P, const BpJob &job, int x,
+                                         int y, int z) {
   const ProjGeom &g = geom[job.proj];
+  const int W = P.W;
   float det[4];
   mat4_vec(g.mvv2m, small_i2f(x), small_i2f(y), small_i2f(z), 1.0f, det);
-  const float qx = (det[0] / det[2]) * sdd;
-  const float qy = (det[1] / det[2]) * sdd;
+  const float qx = (det[0] / det[2]) * P.sdd;
+  const float qy = (det[1] / det[2]) * P.sdd;
   float _px, _py;
-  if (float_ok) {
-    _px = halfWf - qx;
-    _py = halfHf - qy;
-    _px = _px / dsf;
-    _py = _py / dsf;
+  if (P.float_ok) {
+    _px = P.halfWf - qx;
+    _py = P.halfHf - qy;
+    _px = _px / P.dsf;
+    _py = _py / P.dsf;
   } else {
-    _px = (float)(halfW - (double)qx);
-    _py = (float)(halfH - (double)qy);
-    _px = (float)((double)_px / ds);
-    _py = (float)((double)_py / ds);
+    _px = (float)(P.halfW - (double)qx);
+    _py = (float)(P.halfH - (double)qy);
+    _px = (float)((double)_px / P.ds);
+    _py = (float)((double)_py / P.ds);
   }
-  if (!(_px >= 2.0f && _px < wlim && _py >= 2.0f && _py < hlim)) return;
+  if (!(_px >= 2.0f && _px < P.wlim && _py >= 2.0f && _py < P.hlim)) return;
   const float fx = small_floor(_px), fy = small_floor(_py);
   const int px = small_f2i(fx), py = small_f2i(fy);
   const float dx = _px - fx, dy = _py - fy;
@@ -701,22 +714,281 @@ __global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restric
     for (int r = 0; r < 4; ++r) arr[r] = cubic_fast(pv[r][0], pv[r][1], pv[r][2], pv[r][3], dy);
     gv = cubic_fast(arr[0], arr[1], arr[2], arr[3], dx);
   }
-  float *v = job.vol + (x + nx * (y + ny * z));
+  float *v = job.vol + (x + P.nx * (y + P.ny * z));
   if (kMode == 0) {
     float nv;
     if (kExact) {
-      if (!bpc::update_cert(*v, gv, alphaf, alphal, &nv)) nv = (float)((double)*v + alpha * (double)gv);
+      if (!bpc::update_cert(*v, gv, P.alphaf, P.alphal, &nv)) nv = (float)((double)*v + P.alpha * (double)gv);
     } else {
-      nv = __fmaf_rn(alphaf, gv, *v);
+      nv = __fmaf_rn(P.alphaf, gv, *v);
     }
-    nv = mac_max(mac_min(gmax, nv), 0.0f);
+    nv = mac_max(mac_min(P.gmax, nv), 0.0f);
     *v = nv;
   } else {
     *v = *v + gv;
   }
 }
 
+template <bool kExact, int kMode>
+__global__ void __launch_bounds__(256) bp_voxel_kernel(const ProjGeom *__restrict__ geom,
+                                                       const BpJob *__restrict__ jobs, int zblocks, BpParams P) {
+  const int jb = blockIdx.z / zblocks;
+  const BpJob job = jobs[jb];
+  const int x = job.box[0] + blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = job.box[2] + blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = job.box[4] + (blockIdx.z % zblocks) * blockDim.z + threadIdx.z;
+  if (x >= job.box[1] || y >= job.box[3] || z >= job.box[5]) return;
+  bp_voxel<kExact, kMode>(geom, P, job, x, y, z);
+}
+
+BpParams bp_params(const int dims[3], int W, int H, double halfW, double halfH, float sdd, double ds, double alpha,
+                   float gmax) {
+  BpParams P;
+  P.nx = dims[0];
+  P.ny = dims[1];
+  P.W = W;
+  P.H = H;
+  P.halfW = halfW;
+  P.halfH = halfH;
+  P.sdd = sdd;
+  P.ds = ds;
+  P.float_ok = ((double)(float)halfW == halfW && (double)(float)halfH == halfH && (double)(float)ds == ds);
+  P.alpha = alpha;
+  P.gmax = gmax;
+  P.halfWf = (float)halfW;
+  P.halfHf = (float)halfH;
+  P.dsf = (float)ds;
+  P.alphaf = (float)alpha;
+  P.alphal = (float)(alpha - (double)(float)alpha);  // alpha ~ (float)alpha + alphal
+  P.wlim = (float)(W - 2);
+  P.hlim = (float)(H - 2);
+  return P;
+}
+
+// ---------------------------------------------------------------------------
+// Work-queue kernels (wap_internal.h): persistent blocks take items from a
+// counter; an item is one job's pixel tile / voxel block / brick tile, the
+// job found by binary search over the jobs' first items.  No block waits on
+// another, and the per-pixel / per-voxel code is the per-launch kernels'.
+// ---------------------------------------------------------------------------
+template <class J>
+__device__ __forceinline__ int queue_job(const J *__restrict__ jobs, int njobs, int item) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].item0 <= item) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// The next item for the whole block (uniform across its threads).
+__device__ __forceinline__ int queue_next(int *counter, int *slot) {
+  __syncthreads();  // every thread has read the previous item
+  if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) *slot = atomicAdd(counter, 1);
+  __syncthreads();
+  return *slot;
+}
+
+// WX x WY warps, each an 8x4 pixel patch: a tile of 8 WX x 4 WY pixels.
+template <int WX, int WY>
+__global__ void __launch_bounds__(32 * WX * WY) fp_queue_kernel(const QFpJob *__restrict__ jobs, int njobs, int total,
+                                                                int *counter) {
+  __shared__ int slot;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  for (;;) {
+    const int item = queue_next(counter, &slot);
+    if (item >= total) return;
+    const QFpJob &q = jobs[queue_job(jobs, njobs, item)];
+    const int t = item - q.item0, tx = t % q.tiles_x, ty = t / q.tiles_x;
+    const int i = tx * (8 * WX) + (w % WX) * 8 + (lane & 7);
+    const int j = ty * (4 * WY) + (w / WX) * 4 + (lane >> 3);
+    if (i >= q.W || j >= q.H) continue;
+    if (q.bricked)
+      fp_pixel<BrickView>(q.geom, q.job, q.n[0], q.n[1], q.n[2], q.W, q.H, q.sd, q.alpha, i, j);
+    else
+      fp_pixel<VolView>(q.geom, q.job, q.n[0], q.n[1], q.n[2], q.W, q.H, q.sd, q.alpha, i, j);
+  }
+}
+
+template <bool kExact, int kMode, int BX, int BY, int BZ>
+__global__ void __launch_bounds__(BX * BY * BZ) bp_queue_kernel(const QBpJob *__restrict__ jobs, int njobs,
+                                                                int total, int *counter) {
+  __shared__ int slot;
+  const int tx = threadIdx.x % BX, ty = (threadIdx.x / BX) % BY, tz = threadIdx.x / (BX * BY);
+  for (;;) {
+    const int item = queue_next(counter, &slot);
+    if (item >= total) return;
+    const QBpJob &q = jobs[queue_job(jobs, njobs, item)];
+    const int t = item - q.item0;
+    const int bx = t % q.bx, by = (t / q.bx) % q.by, bz = t / (q.bx * q.by);
+    const int x = q.job.box[0] + bx * BX + tx, y = q.job.box[2] + by * BY + ty, z = q.job.box[4] + bz * BZ + tz;
+    if (x >= q.job.box[1] || y >= q.job.box[3] || z >= q.job.box[5]) continue;
+    const BpParams P = *reinterpret_cast<const BpParams *>(&q.P);
+    bp_voxel<kExact, kMode>(q.geom, P, q.job, x, y, z);
+  }
+}
+
+__global__ void __launch_bounds__(256) brick_queue_kernel(const QBrickJob *__restrict__ jobs, int njobs, int total,
+                                                          int *counter) {
+  __shared__ float t[4][4][32];
+  __shared__ int slot;
+  for (;;) {
+    const int item = queue_next(counter, &slot);
+    if (item >= total) return;
+    const QBrickJob &q = jobs[queue_job(jobs, njobs, item)];
+    const int r = item - q.item0, bx = r % q.tx, by = (r / q.tx) % q.ty, bz = r / (q.tx * q.ty);
+    brick_tile(q.vol, q.out, q.n[0], q.n[1], q.n[2], bx * 32, by * 4, bz * 4, t);
+  }
+}
+
+template <class K>
+int resident_blocks(K kernel, int threads) {
+  int per = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0) != cudaSuccess || per < 1) per = 1;
+  return per;
+}
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+  }
+  return n;
+}
+
+// Resident blocks per SM of every work-queue kernel, asked once (so no
+// occupancy query runs while a graph is being captured: warm_queue_kernels).
+struct QueueOcc {
+  int fp[kFpShapes], bp[2][2][kBpShapes], brick;
+};
+const QueueOcc &queue_occ() {
+  static const QueueOcc occ = [] {
+    QueueOcc q;
+    q.fp[0] = resident_blocks(fp_queue_kernel<2, 2>, 128);
+    q.fp[1] = resident_blocks(fp_queue_kernel<1, 2>, 64);
+    q.fp[2] = resident_blocks(fp_queue_kernel<4, 2>, 256);
+#define WAP_OCC(E, M)                                                    \
+  q.bp[E][M][0] = resident_blocks(bp_queue_kernel<E, M, 32, 4, 2>, 256); \
+  q.bp[E][M][1] = resident_blocks(bp_queue_kernel<E, M, 32, 8, 1>, 256); \
+  q.bp[E][M][2] = resident_blocks(bp_queue_kernel<E, M, 32, 2, 4>, 256);
+    WAP_OCC(false, 0)
+    WAP_OCC(false, 1)
+    WAP_OCC(true, 0)
+    WAP_OCC(true, 1)
+#undef WAP_OCC
+    q.brick = resident_blocks(brick_queue_kernel, 256);
+    return q;
+  }();
+  return occ;
+}
+
 }  // namespace
+
+static_assert(sizeof(QBpParams) == sizeof(BpParams), "the host's QBpParams mirrors BpParams");
+
+void warm_queue_kernels() {
+  (void)queue_occ();
+  (void)sm_count();
+}
+
+QBpParams make_bp_params(const int dims[3], int W, int H, double halfW, double halfH, float sdd, double ds,
+                         double alpha, float gmax) {
+  const BpParams P = bp_params(dims, W, H, halfW, halfH, sdd, ds, alpha, gmax);
+  QBpParams Q;
+  std::memcpy(&Q, &P, sizeof(Q));
+  return Q;
+}
+
+void fp_shape_tile(int shape, int &tw, int &th) {
+  tw = shape == 1 ? 8 : shape == 2 ? 32 : 16;
+  th = 8;
+}
+void bp_shape_block(int shape, int &bx, int &by, int &bz) {
+  bx = 32;
+  by = shape == 1 ? 8 : shape == 2 ? 2 : 4;
+  bz = shape == 1 ? 1 : shape == 2 ? 4 : 2;
+}
+
+int fp_queue_items(QFpJob *h, int njobs, int shape) {
+  int tw, th, total = 0;
+  fp_shape_tile(shape, tw, th);
+  for (int j = 0; j < njobs; ++j) {
+    h[j].tiles_x = (h[j].W + tw - 1) / tw;
+    h[j].item0 = total;
+    total += h[j].tiles_x * ((h[j].H + th - 1) / th);
+  }
+  return total;
+}
+int bp_queue_items(QBpJob *h, int njobs, int shape) {
+  int bx, by, bz, total = 0;
+  bp_shape_block(shape, bx, by, bz);
+  for (int j = 0; j < njobs; ++j) {
+    const int *b = h[j].job.box;
+    const int ex = std::max(0, b[1] - b[0]), ey = std::max(0, b[3] - b[2]), ez = std::max(0, b[5] - b[4]);
+    h[j].bx = (ex + bx - 1) / bx;
+    h[j].by = (ey + by - 1) / by;
+    h[j].item0 = total;
+    total += h[j].bx * h[j].by * ((ez + bz - 1) / bz);
+  }
+  return total;
+}
+int brick_queue_items(QBrickJob *h, int njobs) {
+  int total = 0;
+  for (int j = 0; j < njobs; ++j) {
+    h[j].tx = (h[j].n[0] + 31) / 32;
+    h[j].ty = (h[j].n[1] + 3) / 4;
+    h[j].item0 = total;
+    total += h[j].tx * h[j].ty * ((h[j].n[2] + 3) / 4);
+  }
+  return total;
+}
+
+cudaError_t launch_fp_queue(const QFpJob *d_jobs, int njobs, int total, int *d_counter, int shape, cudaStream_t st) {
+  if (njobs <= 0 || total <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const int g = std::min(total, queue_occ().fp[shape == 1 || shape == 2 ? shape : 0] * sm_count());
+  if (shape == 1) fp_queue_kernel<1, 2><<<g, 64, 0, st>>>(d_jobs, njobs, total, d_counter);
+  else if (shape == 2) fp_queue_kernel<4, 2><<<g, 256, 0, st>>>(d_jobs, njobs, total, d_counter);
+  else fp_queue_kernel<2, 2><<<g, 128, 0, st>>>(d_jobs, njobs, total, d_counter);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bp_queue(const QBpJob *d_jobs, int njobs, int total, int *d_counter, int shape, int exact,
+                            int mode, cudaStream_t st) {
+  if (njobs <= 0 || total <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  const int sh = shape == 1 || shape == 2 ? shape : 0;
+  const int g = std::min(total, queue_occ().bp[exact ? 1 : 0][mode ? 1 : 0][sh] * sm_count());
+#define WAP_BPQ(E, M, BX, BY, BZ) \
+  bp_queue_kernel<E, M, BX, BY, BZ><<<g, BX * BY * BZ, 0, st>>>(d_jobs, njobs, total, d_counter);
+#define WAP_BPQ_SHAPE(E, M)                    \
+  if (sh == 1) WAP_BPQ(E, M, 32, 8, 1)         \
+  else if (sh == 2) WAP_BPQ(E, M, 32, 2, 4)    \
+  else WAP_BPQ(E, M, 32, 4, 2)
+  if (exact) {
+    if (mode == 0) WAP_BPQ_SHAPE(true, 0)
+    else WAP_BPQ_SHAPE(true, 1)
+  } else {
+    if (mode == 0) WAP_BPQ_SHAPE(false, 0)
+    else WAP_BPQ_SHAPE(false, 1)
+  }
+#undef WAP_BPQ_SHAPE
+#undef WAP_BPQ
+  return cudaGetLastError();
+}
+
+cudaError_t launch_brick_queue(const QBrickJob *d_jobs, int njobs, int total, int *d_counter, cudaStream_t st) {
+  if (njobs <= 0 || total <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(d_counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  brick_queue_kernel<<<std::min(total, queue_occ().brick * sm_count()), 256, 0, st>>>(d_jobs, njobs, total,
+                                                                                     d_counter);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_forward(const ProjGeom *d_geom, const FpJob *d_jobs, int njobs, const int dims[3], int W, int H,
                            float sd, double alpha, cudaStream_t st, bool bricked) {
@@ -782,14 +1054,9 @@ cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njo
   const dim3 block(32, 4, 2);
   const int zblocks = (maxbox[2] + 1) / 2;
   const dim3 grid((maxbox[0] + 31) / 32, (maxbox[1] + 3) / 4, zblocks * njobs);
-  const int float_ok = ((double)(float)halfW == halfW && (double)(float)halfH == halfH && (double)(float)ds == ds);
   if (W >= (1 << 22) || H >= (1 << 22)) return cudaErrorInvalidValue;
-  const float wlim = (float)(W - 2), hlim = (float)(H - 2);
-  const float alphal = (float)(alpha - (double)(float)alpha);  // alpha ~ (float)alpha + alphal
-#define WAP_BP(E, M)                                                                                             \
-  bp_voxel_kernel<E, M><<<grid, block, 0, st>>>(d_geom, d_jobs, zblocks, dims[0], dims[1], W, H, halfW, halfH, sdd, \
-                                                ds, float_ok, alpha, gmax, (float)halfW, (float)halfH, (float)ds,  \
-                                                (float)alpha, alphal, wlim, hlim)
+  const BpParams P = bp_params(dims, W, H, halfW, halfH, sdd, ds, alpha, gmax);
+#define WAP_BP(E, M) bp_voxel_kernel<E, M><<<grid, block, 0, st>>>(d_geom, d_jobs, zblocks, P)
   if (exact) {
     if (mode == 0) WAP_BP(true, 0);
     else WAP_BP(true, 1);

@@ -92,6 +92,64 @@ cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njo
 // shared-memory slab accumulation of bp_ray_kernel.
 cudaError_t launch_ray_splat(const ProjGeom *d_geom, const SplatJob *d_jobs, int njobs, const int dims[3], int W,
                              int H, float sd, cudaStream_t st, bool direct = false);
+// ---------------------------------------------------------------------------
+// Work-queue forms for a batch of scans of different sizes: one persistent
+// launch covers every job of a step; its blocks take work items (a pixel
+// tile, a voxel block, a brick tile of one job) from a counter that the
+// launcher zeroes first.  Jobs are listed in item order (item0 ascending).
+// ---------------------------------------------------------------------------
+struct QFpJob {
+  FpJob job;
+  const ProjGeom *geom;
+  int n[3], W, H;
+  float sd;
+  double alpha;
+  int bricked;  // job.vol is a brick-layout copy
+  int tiles_x;  // pixel tiles across the detector (set for the launcher's tile shape)
+  int item0;
+};
+struct QBpParams {  // BpParams (projector.cu) as the host fills it
+  int nx, ny, W, H;
+  double halfW, halfH;
+  float sdd;
+  double ds;
+  int float_ok;
+  double alpha;
+  float gmax, halfWf, halfHf, dsf, alphaf, alphal, wlim, hlim;
+};
+struct QBpJob {
+  BpJob job;
+  const ProjGeom *geom;
+  QBpParams P;
+  int bx, by;  // voxel blocks across the box in x and y (the launcher's block shape)
+  int item0;
+};
+struct QBrickJob {
+  const float *vol;  // linear volume
+  float *out;        // its brick-layout copy
+  int n[3];
+  int tx, ty;        // 32x4x4 tiles across x and y
+  int item0;
+};
+QBpParams make_bp_params(const int dims[3], int W, int H, double halfW, double halfH, float sdd, double ds,
+                         double alpha, float gmax);
+// Tile shapes: fp 0 = 16x8 pixels (128 threads), 1 = 8x8 (64), 2 = 32x8 (256);
+// bp 0 = 32x4x2 voxels, 1 = 32x8x1, 2 = 32x2x4 (256 threads).
+constexpr int kFpShapes = 3, kBpShapes = 3;
+void fp_shape_tile(int shape, int &tw, int &th);
+void bp_shape_block(int shape, int &bx, int &by, int &bz);
+// Fill each job's per-shape tile counts and first item in host copies (the
+// caller uploads them); return the launch's item count.
+int fp_queue_items(QFpJob *h_jobs, int njobs, int shape);
+int bp_queue_items(QBpJob *h_jobs, int njobs, int shape);
+int brick_queue_items(QBrickJob *h_jobs, int njobs);
+cudaError_t launch_fp_queue(const QFpJob *d_jobs, int njobs, int total, int *d_counter, int shape, cudaStream_t st);
+cudaError_t launch_bp_queue(const QBpJob *d_jobs, int njobs, int total, int *d_counter, int shape, int exact,
+                            int mode, cudaStream_t st);
+cudaError_t launch_brick_queue(const QBrickJob *d_jobs, int njobs, int total, int *d_counter, cudaStream_t st);
+// Asks every work-queue kernel's occupancy now (before a stream capture).
+void warm_queue_kernels();
+
 // The ray-driven SART update over a job's box: where weight > 0,
 // vol = clamp(vol + alpha * (contrib / weight), 0, gmax) in float.
 struct RayUpdJob {

@@ -121,49 +121,83 @@ def _serve(wap, specs, jobs, rate, budget_gb, workers, flow_bits):
     }
 
 
-def run_batched(wap, torch, n_jobs=12, workers=4, seed=5, budget_gb=150.0):
-    """Batched form: independent scans of uneven sizes (sides from {48, 64,
-    96, 128, 160}, projections uniform in [48, 256], detector 1.5x the side)
-    reconstructed (a) one after another through the plain path, one context
-    at a time, and (b) all submitted at once to the request loop with several
-    workers, so their steps overlap on the GPU.  Returns both wall times and
-    checks that every result is identical."""
+def batched_schedule(wap, frames, flow_iters):
+    """The batched configuration's schedule: 4 CP iterations x 2 SART sweeps
+    (8 sweeps), a 3-level flow (flow_iters primal-dual iterations, 1 warp per
+    level), warp-and-project over every window, the reference's double
+    backprojection."""
+    return wap.reference_schedule(n_cp=4, nb_sart=2, wp_frames=frames, flow_iters=flow_iters, flow_scales=3,
+                                  flow_tol=0.0, flow_warps=1, bp_exact=1)
+
+
+def run_batched(wap, torch, n_jobs=48, seed=5, outer=1, flow_iters=40):
+    """Batched form: n_jobs independent scans of uneven sizes (sides from {48,
+    64, 96, 128, 160}, projections uniform in [48, 256], detector 1.5x the
+    side, frames = projections / 4) reconstructed (a) one after another
+    through the plain path, one context at a time, and (b) together through
+    wap_batch (include/wap/wap_batch.h): the SART steps of every scan in
+    work-queue launches, each CP iteration a replayed CUDA graph, the flows
+    and warp-and-project passes on the scans' own streams.  Returns both wall
+    times (outer iterations of every scan) and checks that every scan's
+    volumes and flows are identical."""
     rng = np.random.default_rng(seed)
     specs = [dict(t=0.0, n=int(rng.choice((48, 64, 96, 128, 160))), nproj=int(rng.integers(48, 257)),
                   seed=2000 + i) for i in range(n_jobs)]
-    jobs = [make_job(wap, torch, s) for s in specs]
+    jobs = []
+    for sp in specs:
+        j = make_job(wap, torch, sp)
+        j["scan"] = wap.make_scan((j["n"],) * 3, tuple(j["scan"].det), sp["nproj"], nframes_cli=max(1, sp["nproj"] // 4))
+        jobs.append(j)
     torch.cuda.synchronize()
+
+    def ctx_of(j):
+        c = wap.Context(j["scan"], j["angles"])
+        c.upload_projections(j["projs"])
+        c.level_setup(0)
+        return c
+
     t0 = time.perf_counter()
     plain = []
     for j in jobs:
-        ctx = wap.Context(j["scan"], j["angles"])
+        ctx = ctx_of(j)
         try:
-            ctx.upload_projections(j["projs"])
-            F = ctx.level_setup(0)
-            ctx.outer_iteration(j["sched"])
-            plain.append([ctx.download_volume(f) for f in range(F)])
+            F = ctx.L.wap_level_nframes(ctx.h)
+            for _ in range(outer):
+                ctx.outer_iteration(batched_schedule(wap, F, flow_iters))
+            plain.append(([ctx.download_volume(f) for f in range(F)], [ctx.download_flow(f) for f in range(F)]))
         finally:
             ctx.close()
     t_loop = time.perf_counter() - t0
-    srv = wap.Server(int(budget_gb * (1 << 30)), workers=workers)
+    ctxs = [ctx_of(j) for j in jobs]
     try:
-        t0 = time.perf_counter()
-        ids = [srv.submit(j["scan"], j["sched"], j["angles"], j["projs"], outer_iterations=1) for j in jobs]
-        for jid in ids:
-            if srv.wait(jid, 3600.0) != wap.WAP_OK:
-                raise wap.WapError("batched job %d failed" % jid)
-        t_batch = time.perf_counter() - t0
+        b = wap.Batch(ctxs)
+        try:
+            scheds = [batched_schedule(wap, c.L.wap_level_nframes(c.h), flow_iters) for c in ctxs]
+            for c in ctxs:
+                c.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(outer):
+                st = b.outer_iteration(scheds)
+            t_batch = time.perf_counter() - t0
+            shapes = b.get_tuning()
+        finally:
+            b.close()
         same = True
-        for jid, j, vols in zip(ids, jobs, plain):
-            n = j["n"]
-            for f, v in enumerate(vols):
-                same = same and np.array_equal(srv.result(jid, f, (n, n, n)), v)
-            srv.release(jid)
+        for c, (vols, flows) in zip(ctxs, plain):
+            c.synchronize()
+            for f in range(len(vols)):
+                same = same and np.array_equal(c.download_volume(f), vols[f]) and np.array_equal(
+                    c.download_flow(f), flows[f])
     finally:
-        srv.close()
-    return {"jobs": n_jobs, "workers": workers, "loop_s": t_loop, "batched_s": t_batch,
-            "speedup": t_loop / t_batch, "identical": bool(same),
-            "sides": sorted(s["n"] for s in specs), "job": "1 outer iteration of the served job schedule"}
+        for c in ctxs:
+            c.close()
+    return {"scans": n_jobs, "outer_iterations": outer, "loop_s": t_loop, "batched_s": t_batch,
+            "speedup": t_loop / t_batch, "identical": bool(same), "tile_shapes": {"fp": shapes[0], "bp": shapes[1]},
+            "launches_per_batch_outer_iteration": int(st.kernel_launches),
+            "sides": {str(k): int(sum(1 for s in specs if s["n"] == k)) for k in (48, 64, 96, 128, 160)},
+            "projections_total": int(sum(s["nproj"] for s in specs)),
+            "job": "4 CP x 2 SART, 3-level flow x %d PD its x 1 warp, WaP over all windows, exact BP; frames = "
+                   "projections / 4" % flow_iters}
 
 
 def run_sequential(wap, torch, n_jobs=3, seed=3, max_side=256, flow_bits=32):

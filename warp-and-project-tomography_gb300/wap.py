@@ -163,6 +163,12 @@ SIGNATURES = {
     "wap_server_now": (_c_double, [_vp]),
     "wap_server_memory": (_c_int, [_vp, ctypes.POINTER(ctypes.c_size_t), ctypes.POINTER(ctypes.c_size_t)]),
     # include/wap/wap_io.h
+    "wap_batch_create": (_c_int, [_vp, _vp, _c_int]),
+    "wap_batch_destroy": (None, [_vp]),
+    "wap_batch_last_error": (ctypes.c_char_p, [_vp]),
+    "wap_batch_outer_iteration": (_c_int, [_vp, _vp, _vp]),
+    "wap_batch_set_tuning": (_c_int, [_vp, _c_int, _c_int]),
+    "wap_batch_get_tuning": (_c_int, [_vp, _vp, _vp]),
     "wap_tiff_info": (_c_int, [ctypes.c_char_p, _vp, _vp, _vp]),
     "wap_tiff_load": (_c_int, [ctypes.c_char_p, _vp, ctypes.c_size_t]),
     "wap_analyze_info": (_c_int, [ctypes.c_char_p, _vp, _vp]),
@@ -441,6 +447,52 @@ class Context:
         self.call("wap_cg_screened_laplacian", d.ctypes.data, a, b, ptr(d_rhs), ptr(d_x), rel_tol, max_iters,
                   abs_tol, mode, ctypes.addressof(it))
         return it.value
+
+
+class Batch:
+    """wap_batch (include/wap/wap_batch.h): scans of uneven sizes reconstructed
+    together, their SART steps in work-queue launches, the CP iteration a CUDA
+    graph, flows and warp-and-project overlapped on the scans' streams.  The
+    contexts are borrowed and must stay open."""
+
+    def __init__(self, contexts):
+        self.L = load()
+        self.contexts = list(contexts)
+        arr = (_vp * len(self.contexts))(*[c.h for c in self.contexts])
+        h = _vp()
+        r = self.L.wap_batch_create(ctypes.byref(h), arr, len(self.contexts))
+        if r != WAP_OK:
+            raise WapError("wap_batch_create failed with status %d" % r)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.wap_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def outer_iteration(self, scheds):
+        arr = (Schedule * len(scheds))(*scheds)
+        st = Stats()
+        r = self.L.wap_batch_outer_iteration(self.h, arr, ctypes.byref(st))
+        if r != WAP_OK:
+            msg = self.L.wap_batch_last_error(self.h)
+            raise WapError("wap_batch_outer_iteration failed (%d): %s" % (r, msg.decode() if msg else ""))
+        return st
+
+    def set_tuning(self, fp_shape=-1, bp_shape=-1):
+        if self.L.wap_batch_set_tuning(self.h, fp_shape, bp_shape) != WAP_OK:
+            raise WapError("wap_batch_set_tuning failed")
+
+    def get_tuning(self):
+        a, b = _c_int(0), _c_int(0)
+        self.L.wap_batch_get_tuning(self.h, ctypes.addressof(a), ctypes.addressof(b))
+        return a.value, b.value
 
 
 def projection_geometry(scan, angle_deg):
