@@ -14,6 +14,7 @@
   flow) against the oracle bit for bit.
 * The precision form at 256^3 against the FP64 oracle.
 * The CP prior kernels alone against the oracle.
+* The projector at the precision configuration's size (512^3 -> 768^2).
 """
 import hashlib
 import json
@@ -300,5 +301,38 @@ def test_cp_prior_bitexact(wapmod, orc, torch_cuda):
                 orc.lib.orc_cp_overrelax(np.array([n] * 3, np.int32), box, x[f], xprev[f], xbar[f])
         for f in range(F):
             assert np.array_equal(ctx.download_volume(f), x[f]), "frame %d" % f
+    finally:
+        ctx.close()
+
+
+# ---------------------------------------------------------------------------
+# 512^3 x 768^2 (the precision configuration's size): the projector
+# ---------------------------------------------------------------------------
+def test_512_projection_bitexact_and_near_fp64(wapmod, orc, torch_cuda):
+    """Forward projections of the 512^3 foam-and-smoke phantom onto a 768^2
+    detector: bit-exact with the oracle (image, ray length, sample count) and
+    within 1e-5 relative L2 of the FP64 oracle."""
+    import oracle as O
+    import precision_512 as P512
+    torch = torch_cuda
+    n, d, nproj = 512, 768, 360
+    vol = P512.phantom(torch, n)
+    torch.cuda.synchronize()
+    h = vol.cpu().numpy()
+    ang = P.golden_angles(nproj)
+    ctx = wapmod.Context(wapmod.make_scan((n, n, n), (d, d), nproj, nframes_cli=3), ang)
+    oscan = O.make_scan((n, n, n), (d, d), nproj, nframes_cli=3)
+    o64 = O.Oracle(fp64=True)
+    try:
+        for k in (0, 121):
+            img, ln, wt = (torch.zeros((d, d), device="cuda") for _ in range(3))
+            torch.cuda.synchronize()
+            ctx.forward(k, vol, img, ln, wt)
+            ctx.synchronize()
+            oi, ol, ow = orc.forward(oscan, ang[k], h)
+            assert np.array_equal(host(wt), ow), "sample counts, projection %d" % k
+            assert np.array_equal(host(ln), ol) and np.array_equal(host(img), oi), "projection %d" % k
+            ref = o64.forward(oscan, ang[k], o64.arr(h))[0]
+            assert rel_l2(host(img), ref) < 1e-5
     finally:
         ctx.close()

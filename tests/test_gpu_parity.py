@@ -489,3 +489,26 @@ def test_precision_form_fp16_flow_state(setup, orc, wapmod):
             assert rel_l2(got, state64["vols"][f]) < 1e-3
     finally:
         ctx.set_tuning("flow_bits", 32)
+
+
+def test_precision_form_projector(setup, orc):
+    """The precision form's SART step: the forward projector reads an FP16
+    brick-layout copy of the volume and sums each ray with Kahan's
+    compensation in FP32 (sample counts unchanged); the FP32 volumes take
+    the updates.  Two sweeps stay within 1e-4 relative L2 of the reference
+    arithmetic (the oracle)."""
+    s = setup
+    ctx = s["ctx"]
+    ctx.level_setup(0)
+    _, st, en, _, _ = orc.level_frames(2, NP, 0)
+    v1 = (s["vol"] * 0.5).astype(np.float32)
+    ctx.upload_volume(1, v1)
+    ctx.set_tuning("flow_bits", 16)
+    try:
+        ctx.sart_prox(1, nb_sart=2, cut=8, exact=1)
+    finally:
+        ctx.set_tuning("flow_bits", 32)
+    got = ctx.download_volume(1)
+    ov, _ = orc.sart_prox(s["oscan"], s["ang"], s["projs"], int(st[1]), int(en[1]), 2, [8, N - 8] * 3, v1.copy())
+    err = rel_l2(got, ov)
+    assert 0 < err < 1e-4, err

@@ -374,6 +374,8 @@ int sart_frames(wap_ctx *ctx, const std::vector<int> &frames, int nb_sart, const
   TRY(upload(ctx, ctx->jobs_fp, fp));
   TRY(upload(ctx, ctx->jobs_bp, bp));
   int mb[3] = {box[1] - box[0], box[3] - box[2], box[5] - box[4]};
+  // The precision form projects FP16 brick copies with compensated sums.
+  const bool half = ctx->flow_bits == 16;
   // Ray-driven mode: each step's corrections are backprojected by the
   // matched ray-driven splat into per-job contribution / weight sums, and
   // the volume takes alpha * contribution / weight (SART's column-sum
@@ -402,9 +404,9 @@ int sart_frames(wap_ctx *ctx, const std::vector<int> &frames, int nb_sart, const
       const int n = step_off[s + 1] - step_off[s];
       if (bricks)
         KL(launch_brick_jobs(ctx->jobs_fp.as<FpJob>() + step_off[s], n, ctx->bricks.as<float>(), ctx->scan.vol,
-                             ctx->stream));
+                             ctx->stream, half));
       KL(launch_forward(ctx->geom.as<ProjGeom>(), (bricks ? ctx->jobs_fpb : ctx->jobs_fp).as<FpJob>() + step_off[s],
-                        n, ctx->scan.vol, W, H, ctx->sd, ctx->scan.alpha, ctx->stream, bricks));
+                        n, ctx->scan.vol, W, H, ctx->sd, ctx->scan.alpha, ctx->stream, bricks, half && bricks));
       ctx->stats.fp_launches++;
       ctx->stats.projections += n;
       ctx->stats.backprojections += n;
@@ -501,9 +503,9 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
     TRY(upload(ctx, ctx->jobs_fpb, fpb));
   }
   KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>(), n, 1, ctx->stream, fast));
-  if (bricks) KL(launch_brick_jobs(ctx->jobs_fp.as<FpJob>(), n, ctx->bricks.as<float>(), d, ctx->stream));
+  if (bricks) KL(launch_brick_jobs(ctx->jobs_fp.as<FpJob>(), n, ctx->bricks.as<float>(), d, ctx->stream, fast));
   KL(launch_forward(ctx->geom.as<ProjGeom>(), (bricks ? ctx->jobs_fpb : ctx->jobs_fp).as<FpJob>(), n, d, W, H, ctx->sd,
-                    ctx->scan.alpha, ctx->stream, bricks));
+                    ctx->scan.alpha, ctx->stream, bricks, fast && bricks));
   ctx->stats.fp_launches++;
   for (const WapItem &it : items)
     CU(cudaMemsetAsync(ctx->delta.as<float>() + (size_t)it.frame * nv, 0, sizeof(float) * nv, ctx->stream));
@@ -1936,9 +1938,10 @@ int batch_plan(wap_batch *b, const wap_schedule *sch, BatchPlan &P, bool dry) {
         q.H = x->scan.det[1];
         q.sd = x->sd;
         q.alpha = x->scan.alpha;
-        q.bricked = 1;
+        q.bricked = x->flow_bits == 16 ? 2 : 1;
         QBrickJob r{};
         r.vol = vol_ptr(x, f);
+        r.half = x->flow_bits == 16 ? 1 : 0;
         for (int a = 0; a < 3; ++a) r.n[a] = x->scan.vol[a];
         slot_of.push_back(slot);
         slot += bf;

@@ -14,6 +14,8 @@
 #include <cstring>
 #include <type_traits>
 
+#include <cuda_fp16.h>
+
 #include "bp_cubic.h"
 #include "wap_internal.h"
 
@@ -36,8 +38,10 @@ struct VolView {
 // z-major inside), so the 32 rays of a warp, which sample a small patch of a
 // plane across the ray direction, gather from a few 256-byte bricks instead
 // of many x rows.  Same clamping, same values: only the address changes.
-struct BrickView {
-  const float *__restrict__ d;
+// T = __half: the precision form's FP16 copy (the taps widen to FP32).
+template <class T>
+struct BrickViewT {
+  const T *__restrict__ d;
   int nx, ny, nz, nbx, nby;
   // The 8 trilinear taps of cell (i, j, k), 0 <= i < nx etc., in the
   // sampler's order, each index +1 clamped to n-1 as VolView::at does: one
@@ -46,20 +50,28 @@ struct BrickView {
   // into the next brick, or 0 at the last cell).
   __device__ __forceinline__ void taps8(int i, int j, int k, float t[8]) const {
     const size_t b = ((size_t)(k >> 2) * nby + (j >> 2)) * nbx + (i >> 2);
-    const float *p = d + (b << 6) + ((k & 3) << 4) + ((j & 3) << 2) + (i & 3);
+    const T *p = d + (b << 6) + ((k & 3) << 4) + ((j & 3) << 2) + (i & 3);
     const int sx = i + 1 > nx - 1 ? 0 : ((i & 3) == 3 ? 61 : 1);
     const int sy = j + 1 > ny - 1 ? 0 : ((j & 3) == 3 ? nbx * 64 - 12 : 4);
     const int sz = k + 1 > nz - 1 ? 0 : ((k & 3) == 3 ? nbx * nby * 64 - 48 : 16);
-    t[0] = __ldg(p);
-    t[1] = __ldg(p + sx);
-    t[2] = __ldg(p + sy);
-    t[3] = __ldg(p + sx + sy);
-    t[4] = __ldg(p + sz);
-    t[5] = __ldg(p + sx + sz);
-    t[6] = __ldg(p + sy + sz);
-    t[7] = __ldg(p + sx + sy + sz);
+    t[0] = ld(p);
+    t[1] = ld(p + sx);
+    t[2] = ld(p + sy);
+    t[3] = ld(p + sx + sy);
+    t[4] = ld(p + sz);
+    t[5] = ld(p + sx + sz);
+    t[6] = ld(p + sy + sz);
+    t[7] = ld(p + sx + sy + sz);
   }
+  static __device__ __forceinline__ float ld(const float *p) { return __ldg(p); }
+  static __device__ __forceinline__ float ld(const __half *p) { return __half2float(__ldg(p)); }
 };
+using BrickView = BrickViewT<float>;
+using BrickViewH = BrickViewT<__half>;
+template <class V>
+struct is_brick : std::false_type {};
+template <class T>
+struct is_brick<BrickViewT<T>> : std::true_type {};
 
 // Trilinear sample with the reference's clamp-then-truncate (SingleScalarVolume.core.h:99-202).
 template <class View>
@@ -75,7 +87,7 @@ struct TrilinearSampler {
     float f1 = 1.0f - f2;
     sumw += 1.0f;
     float tp[8];
-    if constexpr (std::is_same<View, BrickView>::value) {
+    if constexpr (is_brick<View>::value) {
       v.taps8(i, j, k, tp);
     } else {
       tp[0] = v.at(i, j, k);
@@ -164,14 +176,26 @@ __device__ __forceinline__ void produce_ray(const ProjGeom &g, int nx, int ny, i
 
 // CastingRay with one block spanning the whole volume (RayCasterPrepare sets
 // bsize = volume dims, RayCaster.core.h:191-207).
-template <class Sampler>
+// KAHAN (the precision form's projector): the ray sum with Kahan's
+// compensation, so the FP16 samples are summed without FP32 round-off growth.
+template <class Sampler, bool KAHAN = false>
 __device__ __forceinline__ float cast_ray(Sampler &smp, const int n[3], const float vz[4], const float vu[4],
                                           float tnear, float tfar, float sd) {
-  float density = 0.0f;
+  float density = 0.0f, comp = 0.0f;
+  auto add = [&](float v) {
+    if (KAHAN) {
+      const float y = v - comp;
+      const float t = density + y;
+      comp = (t - density) - y;
+      density = t;
+    } else {
+      density += v;
+    }
+  };
   float t1 = tnear;
   const float pos1[3] = {vz[0] + vu[0] * t1, vz[1] + vu[1] * t1, vz[2] + vu[2] * t1};
   const float step[3] = {vu[0] * sd, vu[1] * sd, vu[2] * sd};
-  density += smp(pos1[0], pos1[1], pos1[2]) * sd;
+  add(smp(pos1[0], pos1[1], pos1[2]) * sd);
   float tMax[3], tDelta[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
@@ -194,7 +218,7 @@ __device__ __forceinline__ float cast_ray(Sampler &smp, const int n[3], const fl
     float t = ceilf((t1 - tnear) / sd) * sd + tnear;
     float p0 = vz[0] + vu[0] * t, p1 = vz[1] + vu[1] * t, p2 = vz[2] + vu[2] * t;
     while (t < tb) {
-      density += smp(p0, p1, p2) * sd;
+      add(smp(p0, p1, p2) * sd);
       t += sd;
       p0 += step[0];
       p1 += step[1];
@@ -217,7 +241,19 @@ __device__ __forceinline__ float cast_ray(Sampler &smp, const int n[3], const fl
 // row of the output, so the rows of the tile are read and the bricks written
 // with whole-line accesses through shared memory.  Cells of partial bricks
 // past the grid are written as 0 and never read (indices are clamped first).
-__device__ __forceinline__ void brick_tile(const float *__restrict__ in, float *__restrict__ out, int nx, int ny,
+template <class T>
+__device__ __forceinline__ T to_store(float v);
+template <>
+__device__ __forceinline__ float to_store<float>(float v) {
+  return v;
+}
+template <>
+__device__ __forceinline__ __half to_store<__half>(float v) {
+  return __float2half_rn(v);
+}
+
+template <class T>
+__device__ __forceinline__ void brick_tile(const float *__restrict__ in, T *__restrict__ out, int nx, int ny,
                                            int nz, int x0, int y0, int z0, float (*t)[4][32]) {
   const int tid = threadIdx.x;
   for (int e = tid; e < 512; e += 256) {  // rows in: e = (z * 4 + y) * 32 + x
@@ -232,7 +268,7 @@ __device__ __forceinline__ void brick_tile(const float *__restrict__ in, float *
     const int bx = o >> 6;
     if ((x0 >> 2) + bx >= nbx) continue;
     const int x = (o & 3) + 4 * bx, y = (o >> 2) & 3, z = (o >> 4) & 3;
-    out[(b0 << 6) + o] = t[z][y][x];
+    out[(b0 << 6) + o] = to_store<T>(t[z][y][x]);
   }
 }
 
@@ -244,7 +280,8 @@ __global__ void __launch_bounds__(256) brick_kernel(const float *__restrict__ in
 
 // The volumes of n projection jobs (jobs[j].vol, linear) into consecutive
 // brick-layout slots of bf floats; blockIdx.z runs over z tiles x jobs.
-__global__ void __launch_bounds__(256) brick_jobs_kernel(const FpJob *__restrict__ jobs, float *__restrict__ out,
+template <class T>
+__global__ void __launch_bounds__(256) brick_jobs_kernel(const FpJob *__restrict__ jobs, T *__restrict__ out,
                                                          size_t bf, int nx, int ny, int nz, int ztiles) {
   __shared__ float t[4][4][32];
   const int j = blockIdx.z / ztiles;
@@ -269,7 +306,9 @@ __device__ __forceinline__ void fp_pixel(const ProjGeom *__restrict__ geom, cons
   float vz[4], vu[4], tn, tf;
   produce_ray(g, nx, ny, nz, (float)i, (float)j, vz, vu, tn, tf);
   View view;
-  if constexpr (std::is_same<View, BrickView>::value)
+  if constexpr (std::is_same<View, BrickViewH>::value)
+    view = BrickViewH{reinterpret_cast<const __half *>(job.vol), nx, ny, nz, (nx + 3) >> 2, (ny + 3) >> 2};
+  else if constexpr (std::is_same<View, BrickView>::value)
     view = BrickView{job.vol, nx, ny, nz, (nx + 3) >> 2, (ny + 3) >> 2};
   else
     view = VolView{job.vol, nx, ny, nz};
@@ -277,7 +316,7 @@ __device__ __forceinline__ void fp_pixel(const ProjGeom *__restrict__ geom, cons
   float value = 0.0f, len = 0.0f;
   if (tn < tf) {
     len = tf - tn;
-    value = cast_ray(smp, n, vz, vu, tn, tf, sd);
+    value = cast_ray<TrilinearSampler<View>, std::is_same<View, BrickViewH>::value>(smp, n, vz, vu, tn, tf, sd);
   }
   const int k = i + j * W;
   if (job.img) job.img[k] = value;
@@ -804,7 +843,9 @@ __global__ void __launch_bounds__(32 * WX * WY) fp_queue_kernel(const QFpJob *__
     const int i = tx * (8 * WX) + (w % WX) * 8 + (lane & 7);
     const int j = ty * (4 * WY) + (w / WX) * 4 + (lane >> 3);
     if (i >= q.W || j >= q.H) continue;
-    if (q.bricked)
+    if (q.bricked == 2)
+      fp_pixel<BrickViewH>(q.geom, q.job, q.n[0], q.n[1], q.n[2], q.W, q.H, q.sd, q.alpha, i, j);
+    else if (q.bricked)
       fp_pixel<BrickView>(q.geom, q.job, q.n[0], q.n[1], q.n[2], q.W, q.H, q.sd, q.alpha, i, j);
     else
       fp_pixel<VolView>(q.geom, q.job, q.n[0], q.n[1], q.n[2], q.W, q.H, q.sd, q.alpha, i, j);
@@ -838,7 +879,10 @@ __global__ void __launch_bounds__(256) brick_queue_kernel(const QBrickJob *__res
     if (item >= total) return;
     const QBrickJob &q = jobs[queue_job(jobs, njobs, item)];
     const int r = item - q.item0, bx = r % q.tx, by = (r / q.tx) % q.ty, bz = r / (q.tx * q.ty);
-    brick_tile(q.vol, q.out, q.n[0], q.n[1], q.n[2], bx * 32, by * 4, bz * 4, t);
+    if (q.half)
+      brick_tile(q.vol, reinterpret_cast<__half *>(q.out), q.n[0], q.n[1], q.n[2], bx * 32, by * 4, bz * 4, t);
+    else
+      brick_tile(q.vol, q.out, q.n[0], q.n[1], q.n[2], bx * 32, by * 4, bz * 4, t);
   }
 }
 
@@ -991,10 +1035,12 @@ cudaError_t launch_brick_queue(const QBrickJob *d_jobs, int njobs, int total, in
 }
 
 cudaError_t launch_forward(const ProjGeom *d_geom, const FpJob *d_jobs, int njobs, const int dims[3], int W, int H,
-                           float sd, double alpha, cudaStream_t st, bool bricked) {
+                           float sd, double alpha, cudaStream_t st, bool bricked, bool half) {
   if (njobs <= 0) return cudaSuccess;
   dim3 grid((W + 15) / 16, (H + 7) / 8, njobs);
-  if (bricked) fp_kernel<BrickView><<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
+  if (bricked && half)
+    fp_kernel<BrickViewH><<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
+  else if (bricked) fp_kernel<BrickView><<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
   else fp_kernel<VolView><<<grid, 128, 0, st>>>(d_geom, d_jobs, dims[0], dims[1], dims[2], W, H, sd, alpha);
   return cudaGetLastError();
 }
@@ -1003,12 +1049,19 @@ size_t brick_floats(const int dims[3]) {
   return (size_t)((dims[0] + 3) >> 2) * ((dims[1] + 3) >> 2) * ((dims[2] + 3) >> 2) * 64;
 }
 
-cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const int dims[3], cudaStream_t st) {
+cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const int dims[3], cudaStream_t st,
+                              bool half) {
   if ((size_t)dims[0] * dims[1] * dims[2] == 0 || njobs <= 0) return cudaSuccess;
   const int ztiles = (dims[2] + 3) / 4;
   if ((long long)ztiles * njobs > 65535 || (dims[1] + 3) / 4 > 65535) return cudaErrorInvalidValue;
   const dim3 g((unsigned)((dims[0] + 31) / 32), (unsigned)((dims[1] + 3) / 4), (unsigned)(ztiles * njobs));
-  brick_jobs_kernel<<<g, 256, 0, st>>>(d_jobs, out, brick_floats(dims), dims[0], dims[1], dims[2], ztiles);
+  // the FP16 copies start where the FP32 slots do (brick_floats(dims) floats,
+  // twice as many halves, apart) and fill half of each
+  if (half)
+    brick_jobs_kernel<__half><<<g, 256, 0, st>>>(d_jobs, reinterpret_cast<__half *>(out), 2 * brick_floats(dims),
+                                                 dims[0], dims[1], dims[2], ztiles);
+  else
+    brick_jobs_kernel<float><<<g, 256, 0, st>>>(d_jobs, out, brick_floats(dims), dims[0], dims[1], dims[2], ztiles);
   return cudaGetLastError();
 }
 

@@ -76,15 +76,18 @@ struct SplatJob {
 
 // Launch helpers (implemented in the .cu files).
 // bricked: the jobs' volumes are in the 4x4x4 brick layout (launch_brick).
+// half (the precision form): the brick copies are FP16 and each ray's sum is
+// Kahan-compensated FP32; sample counts and ray lengths are unchanged.
 cudaError_t launch_forward(const ProjGeom *d_geom, const FpJob *d_jobs, int njobs, const int dims[3], int W, int H,
-                           float sd, double alpha, cudaStream_t st, bool bricked = false);
+                           float sd, double alpha, cudaStream_t st, bool bricked = false, bool half = false);
 // Floats of a volume's brick layout (dims rounded up to multiples of 4), and
 // the conversion of a linear volume into it.
 size_t brick_floats(const int dims[3]);
 cudaError_t launch_brick(const float *vol, float *out, const int dims[3], cudaStream_t st);
 // The volumes of njobs projection jobs (d_jobs[j].vol) into slots j of out
 // (brick_floats(dims) floats apart), one launch (njobs <= 65535).
-cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const int dims[3], cudaStream_t st);
+cudaError_t launch_brick_jobs(const FpJob *d_jobs, int njobs, float *out, const int dims[3], cudaStream_t st,
+                              bool half = false);
 cudaError_t launch_bp_voxel(const ProjGeom *d_geom, const BpJob *d_jobs, int njobs, int maxbox[3], const int dims[3],
                             int W, int H, double halfW, double halfH, float sdd, double ds, double alpha, float gmax,
                             int mode, int exact, cudaStream_t st);
@@ -104,7 +107,7 @@ struct QFpJob {
   int n[3], W, H;
   float sd;
   double alpha;
-  int bricked;  // job.vol is a brick-layout copy
+  int bricked;  // 1: job.vol is a brick-layout copy; 2: an FP16 one (the precision form)
   int tiles_x;  // pixel tiles across the detector (set for the launcher's tile shape)
   int item0;
 };
@@ -128,6 +131,7 @@ struct QBrickJob {
   const float *vol;  // linear volume
   float *out;        // its brick-layout copy
   int n[3];
+  int half;          // the copy in FP16 (the precision form)
   int tx, ty;        // 32x4x4 tiles across x and y
   int item0;
 };

@@ -18,6 +18,10 @@ import time
 
 import numpy as np
 
+# The served configuration's accuracy target: a job served in another
+# arithmetic must stay within this relative RMSE of the same job in the
+# reference's arithmetic (the reconstruction-error bound of the precision form).
+RMSE_TARGET = 1e-3
 SIZES = (64, 96, 128, 192, 256)
 WEIGHTS = (0.3, 0.25, 0.2, 0.15, 0.1)
 NPROJS = (64, 128, 192)
@@ -80,7 +84,20 @@ def run(wap, torch, n_jobs=40, rate=20.0, budget_gb=150.0, workers=3, seed=3, ma
     specs = job_stream(n_jobs, rate, seed, max_side)
     jobs = [make_job(wap, torch, s) for s in specs]
     torch.cuda.synchronize()
-    return [_serve(wap, specs, jobs, rate, budget_gb, workers, fb) for fb in flow_bits]
+    runs = [_serve(wap, specs, jobs, rate, budget_gb, workers, fb) for fb in flow_bits]
+    # Accuracy of every form against the first (the reference's arithmetic):
+    # relative RMSE of each job's first-frame volume.
+    base = runs[0].pop("_frame0")
+    for r in runs[1:]:
+        got = r.pop("_frame0")
+        err = np.array([float(np.linalg.norm(g.astype(np.float64) - b) / max(np.linalg.norm(b.astype(np.float64)),
+                                                                             1e-30)) for g, b in zip(got, base)])
+        r["rmse_vs_reference_arithmetic"] = {
+            "measure": "relative RMSE of each job's first-frame volume against the same job served in the "
+                       "reference's arithmetic", "target": RMSE_TARGET,
+            "jobs_within_target": int((err <= RMSE_TARGET).sum()), "max": float(err.max()),
+            "p50": float(np.percentile(err, 50)), "p99": float(np.percentile(err, 99))}
+    return runs
 
 
 def _serve(wap, specs, jobs, rate, budget_gb, workers, flow_bits):
@@ -101,7 +118,9 @@ def _serve(wap, specs, jobs, rate, budget_gb, workers, flow_bits):
                 raise wap.WapError("served job %d failed" % jid)
         infos = [srv.info(jid) for jid in ids]
         _, peak = srv.memory()
-        for jid in ids:
+        frame0 = []
+        for jid, j in zip(ids, jobs):
+            frame0.append(srv.result(jid, 0, (j["n"],) * 3))
             srv.release(jid)
     finally:
         srv.close()
@@ -117,7 +136,7 @@ def _serve(wap, specs, jobs, rate, budget_gb, workers, flow_bits):
         "peak_reserved_gb": peak / float(1 << 30),
         "sides": {str(k): int(sum(1 for s in specs if s["n"] == k)) for k in SIZES},
         "job": "1 outer iteration, frames = projections/8, 2 CP x 2 SART, 2-level flow x 20 PD its, FP32 BP",
-        "flow_bits": flow_bits,
+        "flow_bits": flow_bits, "_frame0": frame0,
     }
 
 
@@ -236,10 +255,19 @@ if __name__ == "__main__":
     import build as _build
     import wap as _wap
 
-    ap = argparse.ArgumentParser(description="served jobs one after another, with per-phase times")
+    ap = argparse.ArgumentParser(description="served jobs one after another, with per-phase times; or, with "
+                                             "--served N, the served stream of N jobs through the request loop in "
+                                             "both arithmetics")
     ap.add_argument("--jobs", type=int, default=3)
     ap.add_argument("--flow-bits", type=int, default=32)
+    ap.add_argument("--served", type=int, default=0)
+    ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--workers", type=int, default=3)
     a = ap.parse_args()
     _build.build()
-    for rec in run_sequential(_wap, _torch, n_jobs=a.jobs, flow_bits=a.flow_bits):
-        print(json.dumps(rec))
+    if a.served:
+        plain, fast = run(_wap, _torch, n_jobs=a.served, rate=a.rate, workers=a.workers, flow_bits=(32, 16))
+        print(json.dumps({"serving": plain, "serving_precision": fast}))
+    else:
+        for rec in run_sequential(_wap, _torch, n_jobs=a.jobs, flow_bits=a.flow_bits):
+            print(json.dumps(rec))
