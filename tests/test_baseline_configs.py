@@ -310,8 +310,11 @@ def test_cp_prior_bitexact(wapmod, orc, torch_cuda):
 # ---------------------------------------------------------------------------
 def test_512_projection_bitexact_and_near_fp64(wapmod, orc, torch_cuda):
     """Forward projections of the 512^3 foam-and-smoke phantom onto a 768^2
-    detector: bit-exact with the oracle (image, ray length, sample count) and
-    within 1e-5 relative L2 of the FP64 oracle."""
+    detector: bit-exact with the oracle (image, ray length, sample count).
+    Against the FP64 oracle the reference's float arithmetic is about 4e-4
+    relative L2 at this size (its sample positions are a float recurrence
+    over some 900 steps per ray, whose drift grows with the grid; 3.5e-6 at
+    32^3): held to 1e-3."""
     import oracle as O
     import precision_512 as P512
     torch = torch_cuda
@@ -333,6 +336,8 @@ def test_512_projection_bitexact_and_near_fp64(wapmod, orc, torch_cuda):
             assert np.array_equal(host(wt), ow), "sample counts, projection %d" % k
             assert np.array_equal(host(ln), ol) and np.array_equal(host(img), oi), "projection %d" % k
             ref = o64.forward(oscan, ang[k], o64.arr(h))[0]
-            assert rel_l2(host(img), ref) < 1e-5
+            err = rel_l2(host(img), ref)
+            print("512^3 projection %d: %.3g relative L2 from the FP64 oracle" % (k, err))
+            assert err < 1e-3
     finally:
         ctx.close()
