@@ -213,6 +213,23 @@ def test_advect_bitexact(setup, orc, dt, box):
     assert np.array_equal(host(out), ref)
 
 
+@pytest.mark.parametrize("extreme", ["huge", "nan"])
+def test_advect_bitexact_with_extreme_velocity(setup, orc, extreme):
+    """A velocity field the cell-centre shortcut must not take (a component at
+    or above 2^124, or a NaN): the warp falls back to the full clamped
+    tricubic everywhere and still gives the oracle's result."""
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    aabb = np.array([0, N, 0, N, 0, N], np.float32)
+    flow = s["flow"].copy()
+    flow[1, 3, 4, 5] = 3.0e37 if extreme == "huge" else np.nan
+    out = torch.zeros((1, N, N, N), device="cuda")
+    ctx.advect([N, N, N], aabb, dev(torch, flow), dev(torch, s["vol"]), 1, 0.7, out)
+    ctx.synchronize()
+    ref = orc.advect([N, N, N], aabb, flow, s["vol"], 0.7)
+    assert np.array_equal(host(out), ref.reshape(1, N, N, N), equal_nan=True)
+
+
 def test_blur_and_resize_bitexact(setup, orc):
     s = setup
     torch, ctx = s["torch"], s["ctx"]

@@ -164,15 +164,37 @@ __device__ __forceinline__ void sample3(const float *__restrict__ vel, size_t nv
     out[c] = std_max(mn[c], std_min(mx[c], cubf<FAST>(p[c][0], p[c][1], p[c][2], p[c][3], s.dz)));
 }
 
+// 1 in bad[j] when job j's velocity field has a component that is NaN or
+// has |v| >= 2^124 (the advect kernel's centre shortcut needs neither).
+__global__ void __launch_bounds__(256) vel_range_kernel(const AdvectJob *__restrict__ jobs, size_t n3, int *bad) {
+  const float *__restrict__ v = jobs[blockIdx.y].vel;
+  int b = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n3; i += (size_t)gridDim.x * blockDim.x)
+    b |= (__float_as_uint(__ldg(v + i)) & 0x7fffffffu) >= 0x7d800000u;
+  if (__syncthreads_or(b) && threadIdx.x == 0) bad[blockIdx.y] = 1;
+}
+
+// The velocity at a sample point that sits exactly on a cell centre (every
+// interpolation weight zero): there each of CImg's cubics c + 0.5 (t (..) +
+// t^2 (..) + t^3 (..)) with t = 0, and the Horner form of the precision
+// form, is its centre tap c, as long as no bracketed term is NaN or
+// overflows (the taps are below 2^124 in magnitude, so each term stays below
+// 12 * 2^124 < 2^128), up to the sign of a zero result; and the limiter
+// keeps c, which is one of its 8 cells.  The trace uses the velocity only as
+// p + dt v with p a positive cell-centre coordinate, so a zero's sign cannot
+// change the output: the centre tap gives the reference's bits.
 template <bool FAST>
 __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__restrict__ wx,
                                                      const float *__restrict__ wy, const float *__restrict__ wz,
-                                                     const AdvectJob *__restrict__ jobs, int nc) {
+                                                     const AdvectJob *__restrict__ jobs, int nc,
+                                                     const int *__restrict__ bad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z % G.n[2];
-  const AdvectJob job = jobs[blockIdx.z / G.n[2]];
+  const int jb = blockIdx.z / G.n[2];
+  const AdvectJob job = jobs[jb];
   if (i >= G.n[0] || j >= G.n[1]) return;
+  const bool centre_ok = bad && !bad[jb];
   const float *__restrict__ vel = job.vel;
   const float *__restrict__ src = job.src;
   float *__restrict__ out = job.out;
@@ -182,7 +204,13 @@ __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__
   // trace (advection.h:101-115) with dt_trace = -dt.
   SamplePoint s = locate(G, p[0], p[1], p[2]);
   float v[3];
-  sample3<FAST>(vel, nv, G, s, v);
+  if (centre_ok && s.dx == 0.0f && s.dy == 0.0f && s.dz == 0.0f) {
+    const size_t c = s.xs[1] + (size_t)G.n[0] * (s.ys[1] + (size_t)G.n[1] * s.zs[1]);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) v[ch] = __ldg(vel + ch * nv + c);
+  } else {
+    sample3<FAST>(vel, nv, G, s, v);
+  }
   const float p2[3] = {p[0] + tdt * v[0], p[1] + tdt * v[1], p[2] + tdt * v[2]};
   s = locate(G, p2[0], p2[1], p2[2]);
   sample3<FAST>(vel, nv, G, s, v);
@@ -235,8 +263,19 @@ void world_table(const int dims[3], const float aabb[6], float *h) {
 }
 
 cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d_world, const AdvectJob *d_jobs,
-                          int njobs, int nc, cudaStream_t st, bool fast) {
+                          int njobs, int nc, cudaStream_t st, bool fast, int *d_flags) {
   if (njobs <= 0) return cudaSuccess;
+  if (d_flags) {  // the range check of each job's velocity (the centre shortcut's condition)
+    cudaError_t e = cudaMemsetAsync(d_flags, 0, sizeof(int) * njobs, st);
+    if (e != cudaSuccess) return e;
+    const size_t n3 = 3 * (size_t)dims[0] * dims[1] * dims[2];
+    const unsigned gx = (unsigned)std::min<size_t>((n3 + 255) / 256, 1216);
+    for (int j = 0; j < njobs; j += 65535) {
+      vel_range_kernel<<<dim3(gx, (unsigned)std::min(65535, njobs - j)), 256, 0, st>>>(d_jobs + j, n3, d_flags + j);
+      e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+    }
+  }
   Grid3 G;
   for (int a = 0; a < 3; ++a) {
     G.n[a] = dims[a];
@@ -250,12 +289,13 @@ cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d
   for (int j = 0; j < njobs; j += per) {
     const int n = std::min(per, njobs - j);
     const dim3 grid((dims[0] + 31) / 32, (dims[1] + 3) / 4, dims[2] * n);
+    const int *bad = d_flags ? d_flags + j : nullptr;
     if (fast)
       advect_kernel<true><<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1], d_jobs + j,
-                                                  nc);
+                                                  nc, bad);
     else
       advect_kernel<false><<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1],
-                                                   d_jobs + j, nc);
+                                                   d_jobs + j, nc, bad);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

@@ -205,6 +205,7 @@ struct wap_ctx {
   DevMem blur_a, blur_b, rs_a, rs_b;
   DevMem pyr_b1, pyr_b2;  // blurred full-size flow inputs
   DevMem adv_tab;         // cell-centre table of a wap_advect call
+  DevMem adv_flags;       // per advect job: its velocity's range check
   DevMem bricks;          // brick-layout copies of the volumes a projection batch reads
   DevMem jobs_fpb;        // the batch's projection jobs pointing at those copies
   int fp_bricks = 1;      // 1: the forward projector reads brick-layout copies (same bits, faster)
@@ -502,7 +503,9 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
     for (int q = 0; q < n; ++q) fpb[q].vol = ctx->bricks.as<float>() + q * bf;
     TRY(upload(ctx, ctx->jobs_fpb, fpb));
   }
-  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>(), n, 1, ctx->stream, fast));
+  CU(ctx->adv_flags.ensure(sizeof(int) * 2 * n));
+  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>(), n, 1, ctx->stream, fast,
+                   ctx->adv_flags.as<int>()));
   if (bricks) KL(launch_brick_jobs(ctx->jobs_fp.as<FpJob>(), n, ctx->bricks.as<float>(), d, ctx->stream, fast));
   KL(launch_forward(ctx->geom.as<ProjGeom>(), (bricks ? ctx->jobs_fpb : ctx->jobs_fp).as<FpJob>(), n, d, W, H, ctx->sd,
                     ctx->scan.alpha, ctx->stream, bricks, fast && bricks));
@@ -512,7 +515,8 @@ int wap_step(wap_ctx *ctx, const std::vector<WapItem> &items, int exact) {
   int mb[3] = {d[0], d[1], d[2]};
   KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_bp.as<BpJob>(), n, mb, d, W, H, ctx->halfW, ctx->halfH,
                      (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha, ctx->gmax, 1, exact, ctx->stream));
-  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + n, n, 1, ctx->stream, fast));
+  KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + n, n, 1, ctx->stream, fast,
+                   ctx->adv_flags.as<int>() + n));
   ctx->stats.advect_voxels += 2.0 * n * (double)nv;
   ctx->stats.projections += n;
   ctx->stats.backprojections += n;
@@ -571,18 +575,19 @@ int adaptive_warp(wap_ctx *ctx, int f, int nb_warp, int cut, int exact) {
   int mb[3] = {box[1] - box[0], box[3] - box[2], box[5] - box[4]};
   const bool fast = ctx->flow_bits == 16;
   CU(cudaMemsetAsync(dual, 0, sizeof(float) * np, ctx->stream));
+  CU(ctx->adv_flags.ensure(sizeof(int) * 2));
   for (int it = 1; it <= nb_warp; ++it) {
     CU(cudaMemsetAsync(delta, 0, sizeof(float) * nv, ctx->stream));
     for (int q = 0; q < n; ++q) {
       KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + 2 * q, 1, 1, ctx->stream,
-                       fast));
+                       fast, ctx->adv_flags.as<int>()));
       KL(launch_forward(ctx->geom.as<ProjGeom>(), ctx->jobs_fp.as<FpJob>() + q, 1, d, W, H, ctx->sd, ctx->scan.alpha,
                         ctx->stream, false));
       KL(launch_bp_voxel(ctx->geom.as<ProjGeom>(), ctx->jobs_bp.as<BpJob>() + q, 1, mb, d, W, H, ctx->halfW,
                          ctx->halfH, (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha, ctx->gmax, 1, exact,
                          ctx->stream));
       KL(launch_advect(d, aabb, ctx->world.as<float>(), ctx->jobs_adv.as<AdvectJob>() + 2 * q + 1, 1, 1, ctx->stream,
-                       fast));
+                       fast, ctx->adv_flags.as<int>() + 1));
       KL(launch_wap_accumulate(nv, vol, back, ctx->scan.alpha, ctx->gmax, ctx->stream, false));
       ctx->stats.fp_launches++;
       ctx->stats.projections++;
@@ -930,8 +935,9 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     aj.vel = vcur;
     std::vector<AdvectJob> ajs{aj};
     TRY(upload(ctx, ctx->jobs_misc, ajs));
+    CU(ctx->adv_flags.ensure(sizeof(int) * 2));
     KL(launch_advect(dims, aabb, w->world.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, 1, ctx->stream,
-                     ctx->flow_bits == 16));
+                     ctx->flow_bits == 16, ctx->adv_flags.as<int>()));
     ctx->stats.advect_voxels += (double)nv;
     KL(launch_linearize(D, w->warp.as<float>(), I1, vcur, w->u.as<float>(), w->kx4prev.as<float>(), ctx->stream));
     if (half) KL(launch_to_pairs(nv, 4, w->u.as<float>(), w->uh.p, ctx->stream));
@@ -1641,7 +1647,9 @@ int wap_advect(wap_ctx *ctx, const int *dims, const float *aabb, const float *d_
   TRY(upload(ctx, ctx->adv_tab, h));
   std::vector<AdvectJob> jobs{AdvectJob{d_vel, d_src, d_out, dt}};
   TRY(upload(ctx, ctx->jobs_misc, jobs));
-  KL(launch_advect(dims, aabb, ctx->adv_tab.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, nc, ctx->stream));
+  CU(ctx->adv_flags.ensure(sizeof(int) * 2));
+  KL(launch_advect(dims, aabb, ctx->adv_tab.as<float>(), ctx->jobs_misc.as<AdvectJob>(), 1, nc, ctx->stream, false,
+                   ctx->adv_flags.as<int>()));
   CU(cudaStreamSynchronize(ctx->stream));  // the host table and job list are reused by the next call
   return WAP_OK;
 }

@@ -177,8 +177,11 @@ struct AdvectJob {
 void world_table(const int dims[3], const float aabb[6], float *h);
 // fast: the precision form's fused-multiply-add cubic (results within a
 // tolerance); false: the reference's arithmetic, bit for bit.
+// d_flags (njobs ints of scratch, may be NULL): with it, each job's velocity
+// is range-checked first and cell-centre samples take their centre tap (same
+// bits); without it every sample is the full clamped tricubic.
 cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d_world, const AdvectJob *d_jobs,
-                          int njobs, int nc, cudaStream_t st, bool fast = false);
+                          int njobs, int nc, cudaStream_t st, bool fast = false, int *d_flags = nullptr);
 // vol = clamp_cut(vol + alpha*adv) then max(vol*roi, 0) (WaP_Tomo.cpp:1378-1412);
 // floor = false leaves out the max(., 0).
 cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st,
