@@ -10,7 +10,7 @@ bandwidth against the kernel's algorithmic bytes:
           62 B per voxel in the precision form (--flow-bits 16, FP16 pairs)
   fp      forward projection, V*4 + 16*D bytes (volume once, 4 outputs per pixel)
   bp      voxel-driven backprojection over the ROI, 2*V*4 + 4*D bytes
-  advect  one warp of a 1-channel volume by a 3-channel flow, V*(2+3)*4 bytes
+  advect  one warp of a 1-channel volume by a smooth 3-channel flow, V*(2+3)*4 bytes
   bp_ray  ray-driven matched backprojection (contribution and weight sums,
           read and written once each: 16*V + 4*D bytes), --splat-form 1 for the
           one-global-atomic-per-tap form
@@ -108,7 +108,11 @@ def main():
         ms = timed(lambda: ctx.backproject_ray(3, corr, con, wsum), a.reps)
         report("bp_ray", ms, 16 * nv + 4 * d * d, {"splat_form": a.splat_form})
     if a.kernel in ("advect", "all"):
-        flow = torch.randn((3, n, n, n), device="cuda", generator=g) * 2
+        # a smooth flow of up to 4 voxels (a random 8^3 lattice interpolated
+        # trilinearly), like the displacement fields the solver warps by
+        lat = torch.rand((3, 1, 8, 8, 8), device="cuda", generator=g) * 8 - 4
+        flow = torch.nn.functional.interpolate(lat, size=(n, n, n), mode="trilinear",
+                                               align_corners=True)[:, 0].contiguous()
         out = torch.zeros((1, n, n, n), device="cuda")
         ms = timed(lambda: ctx.advect([n, n, n], [0, n, 0, n, 0, n], flow, vol, 1, 0.7, out), a.reps)
         report("advect", ms, nv * 5 * 4)
