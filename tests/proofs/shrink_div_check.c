@@ -5,7 +5,9 @@
  * inputs a, the fast path where its guard accepts a and the scaled path for
  * 0 < |a| < 1e-30 must give the bits of the IEEE quotient a / den.  The GPU
  * repeats the same proof on the device before it uses the fast path; this
- * host run pins the algorithm for a range of lambdas without a GPU.
+ * host run pins the algorithm for a range of lambdas without a GPU.  With
+ * the argument "sigma1" the divisor is sigma1 itself, which the residual
+ * iterations divide nine dual terms by.
  * Prints the mismatch counts; exit status 1 if any. */
 #include <math.h>
 #include <stdint.h>
@@ -33,9 +35,10 @@ __attribute__((noinline)) static float shrink_tiny(float a, float den, float rin
   return t;
 }
 int main(int argc, char **argv) {
-  const float lambda = argc > 1 ? strtof(argv[1], 0) : 0.05f;
+  const int by_sigma1 = argc > 1 && strcmp(argv[1], "sigma1") == 0;
+  const float lambda = argc > 1 && !by_sigma1 ? strtof(argv[1], 0) : 0.05f;
   const float sigma1 = 1.0f / 3.0f;
-  const float den = lambda + 2 * sigma1, rinv = 1.0f / den;
+  const float den = by_sigma1 ? sigma1 : lambda + 2 * sigma1, rinv = 1.0f / den;
   unsigned long long bad_fast = 0, bad_tiny = 0, n_tiny = 0, n_ieee = 0;
   #pragma omp parallel for reduction(+:bad_fast,bad_tiny,n_tiny,n_ieee) schedule(static)
   for (long long i = 0; i < (1LL << 32); ++i) {

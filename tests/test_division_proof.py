@@ -1,7 +1,8 @@
 """The division-free shrink of the primal-dual kernels, proved on the host:
 the fast path (where its range guard accepts the input) and the scaled path
 for tiny inputs reproduce the IEEE quotient a / den bit for bit over all 2^32
-float inputs, for the reference's lambda and a spread of others.  The device
+float inputs, for the reference's lambda and a spread of others, and for
+the divisor sigma1 of the residual's dual terms.  The device
 runs the same proof (pd_fastdiv_check_kernel) before it takes the fast path;
 this test pins the algorithm without a GPU."""
 import os
@@ -30,7 +31,7 @@ def checker(tmp_path_factory):
     return exe
 
 
-@pytest.mark.parametrize("lam", ["0.05", "7.5"])
+@pytest.mark.parametrize("lam", ["0.05", "7.5", "sigma1"])
 def test_shrink_division_exact_for_every_float(checker, lam):
     r = subprocess.run([checker, lam], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr

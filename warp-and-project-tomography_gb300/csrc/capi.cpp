@@ -854,7 +854,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
   std::memcpy(&den_bits, &den, 4);
   // Proofs are per device and shared by every context in the process
   // (key 0: the reciprocal; otherwise the divisor's bits).
-  auto proven = [&](uint64_t key, int &out) -> int {
+  auto proven = [&](uint64_t key, float dv, int &out) -> int {
     {
       std::lock_guard<std::mutex> lk(g_proof_mutex);
       auto it = g_proofs.find(std::make_pair(ctx->device, key));
@@ -866,7 +866,7 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     DevMem bad;
     CU(bad.ensure(sizeof(unsigned long long)));
     if (key == 0) KL(launch_pd_rcp_check(bad.as<unsigned long long>(), ctx->stream));
-    else KL(launch_pd_fastdiv_check(den, rinv, bad.as<unsigned long long>(), ctx->stream));
+    else KL(launch_pd_fastdiv_check(dv, 1.0f / dv, bad.as<unsigned long long>(), ctx->stream));
     unsigned long long nbad = 1;
     CU(cudaMemcpyAsync(&nbad, bad.p, sizeof(nbad), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
@@ -875,9 +875,15 @@ int flow_level(wap_ctx *ctx, const int dims[3], const float *I1, const float *I2
     g_proofs[std::make_pair(ctx->device, key)] = out;
     return WAP_OK;
   };
-  int fastdiv = 0, rcp = 0;
-  TRY(proven(((uint64_t)1 << 32) | den_bits, fastdiv));
-  TRY(proven(0, rcp));
+  // fastdiv bit 0: the shrink's divisor den; bit 1: the residual's sigma1
+  // (the TMA form's residual iterations divide nine dual terms by it)
+  int fastdiv = 0, fast_s = 0, rcp = 0;
+  uint32_t s1_bits;
+  std::memcpy(&s1_bits, &sigma1, 4);
+  TRY(proven(((uint64_t)1 << 32) | den_bits, den, fastdiv));
+  TRY(proven(((uint64_t)1 << 32) | s1_bits, sigma1, fast_s));
+  TRY(proven(0, 0.0f, rcp));
+  fastdiv |= fast_s << 1;
   int form = 0, zchunk = 0;
   if (w->tma_state == 0) {
     w->tma_state = -1;
