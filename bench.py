@@ -23,8 +23,10 @@ from pinned memory and its results (volume and flow) copied back.
 --impl reference times the reference algorithm on the host CPU (the oracle
 port of the reference's OpenMP code) on a bounded sample: one forward and
 back projection, one warp, one CP frame pass and a few primal-dual iterations
-at full size per step, composed into outer-iter/s from the exact op counts of
-the GPU run's schedule.
+at full size per step (ms_per_step is that sample's wall time), composed into
+outer-iter/s from the op counts of one whole outer iteration measured on the
+GPU (outer_iteration_counts_256.json in the package; the GPU path performs the
+reference's operations bit for bit, so the counts are the reference's too).
 """
 import argparse
 import json
@@ -90,7 +92,44 @@ def parse():
                     help="timed launches per kernel of the line's per-kernel roofline table (0: skip)")
     ap.add_argument("--full-outer", action="store_true",
                     help="also time one whole outer iteration (all frames in pass order; minutes at 256^3)")
+    ap.add_argument("--save-outer-counts", default="",
+                    help="with --full-outer: write that outer iteration's op counts to this JSON file (the counts "
+                         "the CPU legs compose their outer-iter/s from)")
     return ap.parse_args()
+
+
+# Op counts of one whole outer iteration of the default workload, measured by
+# `python bench.py --full-outer --save-outer-counts <this file>` on a GB300.
+# The GPU path is bit-exact with the reference, so the reference performs the
+# same operations (in particular the same primal-dual iterations per level,
+# which the tolerance stops early on the coarse levels).
+OUTER_COUNTS = os.path.join(PKG, "outer_iteration_counts_256.json")
+COUNT_KEYS = ("projections", "backprojections", "advect_voxels", "cp_frame_passes", "pd_voxel_iters")
+
+
+def outer_counts(args):
+    """The measured counts when the workload is the default one, else None."""
+    if (args.n, args.det, args.nproj, args.scales, args.flow_iters) != (256, 384, 192, 4, 3000):
+        return None
+    try:
+        with open(OUTER_COUNTS) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    return {k: float(d["op_counts"][k]) for k in COUNT_KEYS}
+
+
+def bench_config(args, F):
+    """The workload's config object, shared by both arms."""
+    return {"workload": "256^3 volume, 192 proj at 384^2, 48 frames, 5 CP x 2 SART, 4-level L1-TV flow "
+                        "(tol 0.008, <=3000 its, 3 warps), WaP over all windows; step = one frame's share "
+                        "of an outer iteration" if (args.n, args.det, args.nproj) == (256, 384, 192) else
+                        "%d^3 volume, %d proj at %d^2, %d frames, 5 CP x 2 SART, %d-level L1-TV flow (tol 0.008, "
+                        "<=%d its, 3 warps), WaP over all windows; step = one frame's share of an outer iteration"
+                        % (args.n, args.nproj, args.det, F, args.scales, args.flow_iters),
+            "volume": [args.n] * 3, "detector": [args.det] * 2, "projections": args.nproj, "frames": F,
+            "parallelism": "single", "l2": "working set > L2 (GBs per step)",
+            "bp_arithmetic": "reference double (exact)"}
 
 
 def dist_init(args):
@@ -242,9 +281,9 @@ def cpu_sample(args, counts, threads):
     sec = (counts["projections"] * t["fp"] + counts["backprojections"] * t["bp"] +
            counts["advect_voxels"] / nv * t["advect"] + counts["cp_frame_passes"] * t["cp"] +
            counts["pd_voxel_iters"] * t["pd_voxel_iter"])
-    sample = ("composed from one 256^3->384^2 forward projection, one bicubic backprojection, one warp, one CP "
-              "frame pass and 4 timed primal-dual iterations at 256^3 (OpenMP, all host cores), weighted by the op "
-              "counts of one outer iteration")
+    sample = ("composed from one %d^3->%d^2 forward projection, one bicubic backprojection, one warp, one CP "
+              "frame pass and %d timed primal-dual iterations at %d^3 (OpenMP, all host cores), weighted by the op "
+              "counts of one outer iteration" % (n, args.det, pd_its, n))
     return sec, t, sample
 
 
@@ -470,17 +509,22 @@ def run_gb300(args):
         full = {"seconds": sec, "value": 1.0 / sec, "unit": "outer-iter/s", "wall_seconds": time.time() - w0,
                 "pd_iterations": int(so.flow_pd_iterations), "phase_ms": {"cp_sart": so.ms_cp, "flow": so.ms_flow,
                                                                          "wap": so.ms_wap},
+                "pd_iterations_per_level": [int(so.pd_iters_level[l]) for l in range(args.scales)],
+                "op_counts": {k: float(getattr(so, k)) for k in COUNT_KEYS},
                 "note": "one wap_outer_iteration over all %d frames, CUDA events on the library's stream" % F}
+        if rank == 0 and args.save_outer_counts:
+            with open(args.save_outer_counts, "w") as f:
+                json.dump({"workload": bench_config(args, F)["workload"],
+                           "made_by": "python bench.py --full-outer --save-outer-counts <file> (one GB300)",
+                           "outer_iteration_seconds": sec, "pd_iterations": full["pd_iterations"],
+                           "pd_iterations_per_level_finest_first": full["pd_iterations_per_level"],
+                           "op_counts": full["op_counts"]}, f, indent=1)
+                f.write("\n")
     result = {
         "metric": METRIC, "value": value, "unit": "outer-iter/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": t_dev / K * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded foam phantom, RBF+compression, Poisson I0=1e4)",
-        "config": {"workload": "256^3 volume, 192 proj at 384^2, 48 frames, 5 CP x 2 SART, 4-level L1-TV flow "
-                               "(tol 0.008, <=3000 its, 3 warps), WaP over all windows; step = one frame's share "
-                               "of an outer iteration",
-                   "volume": [n, n, n], "detector": [d, d], "projections": args.nproj, "frames": F,
-                   "parallelism": "replicas" if world > 1 else "single", "l2": "working set > L2 (GBs per step)",
-                   "bp_arithmetic": "reference double (exact)"},
+        "config": dict(bench_config(args, F), parallelism="replicas" if world > 1 else "single"),
         "e2e": {"value": e2e, "unit": "outer-iter/s", "h2d_bytes_per_step": h2d_bytes // K,
                 "d2h_bytes_per_step": 4 * nv * 4},
         "gpu_launches": int(agg["kernel_launches"]),
@@ -518,12 +562,17 @@ def run_gb300(args):
     if args.flow_bits == 16:
         result["dtype"] = "f32 arithmetic, f16 flow state"
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        counts = {k: agg[k] * F / K for k in ("projections", "backprojections", "advect_voxels", "cp_frame_passes",
-                                               "pd_voxel_iters")}
+        counts = outer_counts(args)
+        source = "measured counts of one whole outer iteration (%s)" % os.path.relpath(OUTER_COUNTS, REPO)
+        if counts is None:
+            counts = {k: agg[k] * F / K for k in COUNT_KEYS}
+            source = "counts of the timed frame-steps, times frames / steps"
         threads = os.cpu_count() or 1
+        w0 = time.time()
         sec, parts, sample = cpu_sample(args, counts, threads)
         result["cpu_baseline"] = {"value": 1.0 / sec, "unit": "outer-iter/s", "cores": threads, "kind": "port",
-                                  "sample": sample, "component_seconds": parts}
+                                  "sample": sample + "; " + source, "sample_seconds": time.time() - w0,
+                                  "composed_seconds_per_outer_iteration": sec, "component_seconds": parts}
     if rank == 0 and world == 1 and (args.serve_jobs > 0 or args.batch_jobs > 0):
         del projs
         ctx.close()
@@ -552,33 +601,46 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    # Op counts of one outer iteration of the same schedule at 256^3 x 192
-    # (48 frames, windows of <= 7, 5 CP x 2 SART, 3 warps, 4 levels).
     import oracle as O
     orc = O.Oracle()
     F = args.nproj // 4
-    nf, st, en, ft, tu = orc.level_frames(F, args.nproj, 0)
-    win = (en - st + 1).astype(np.int64)
-    n = args.n
-    nv = n ** 3
-    lvl = sum((1.0 / 8 ** l) for l in range(args.scales))
-    counts = {"projections": int(5 * 2 * win.sum() + win.sum()), "backprojections": int(5 * 2 * win.sum() + win.sum()),
-              "advect_voxels": float(2 * win.sum() * nv + (F - 1) * 3 * lvl * nv),
-              "cp_frame_passes": 5 * F, "pd_voxel_iters": float((F - 1) * 3 * (args.flow_iters + 1) * lvl * nv)}
+    counts = outer_counts(args)
+    source = "measured counts of one whole outer iteration (%s)" % os.path.relpath(OUTER_COUNTS, REPO)
+    if counts is None:
+        # Op counts of one outer iteration of the same schedule from its
+        # structure (windows of <= 7, 5 CP x 2 SART, 3 warps, every flow level
+        # at its iteration cap: an upper bound on the primal-dual work).
+        nf, st, en, ft, tu = orc.level_frames(F, args.nproj, 0)
+        win = (en - st + 1).astype(np.int64)
+        nv = args.n ** 3
+        lvl = sum((1.0 / 8 ** l) for l in range(args.scales))
+        counts = {"projections": float(5 * 2 * win.sum() + win.sum()),
+                  "backprojections": float(5 * 2 * win.sum() + win.sum()),
+                  "advect_voxels": float(2 * win.sum() * nv + (F - 1) * 3 * lvl * nv),
+                  "cp_frame_passes": float(5 * F),
+                  "pd_voxel_iters": float((F - 1) * 3 * (args.flow_iters + 1) * lvl * nv)}
+        source = "op counts from the schedule's structure, every flow level at its iteration cap"
     threads = os.cpu_count() or 1
-    times = []
+    composed, walls, parts = [], [], None
     for i in range(args.warmup + args.steps):
+        w0 = time.time()
         sec, parts, sample = cpu_sample(args, counts, threads)
         if i >= args.warmup:
-            times.append(sec)
-    sec = float(np.mean(times))
+            composed.append(sec)
+            walls.append(time.time() - w0)
+    sec = float(np.mean(composed))
     v = 1.0 / sec
+    # A step is one bounded CPU sample of the workload (its wall time is
+    # ms_per_step); value is outer-iter/s composed from the sample's component
+    # times and the op counts of one outer iteration.
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "outer-iter/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "256^3 volume, 192 proj at 384^2, 48 frames (composed CPU sample)"},
-        "cpu_baseline": {"value": v, "unit": "outer-iter/s", "cores": threads, "kind": "port", "sample": sample},
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(walls)) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": bench_config(args, F),
+        "cpu_baseline": {"value": v, "unit": "outer-iter/s", "cores": threads, "kind": "port",
+                         "sample": sample + "; " + source, "composed_seconds_per_outer_iteration": sec,
+                         "component_seconds": parts},
         "e2e": {"value": v, "unit": "outer-iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }))
