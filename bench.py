@@ -22,8 +22,9 @@ from pinned memory and its results (volume and flow) copied back.
 
 --impl reference times the reference algorithm on the host CPU (the oracle
 port of the reference's OpenMP code) on a bounded sample: one forward and
-back projection, one warp, one CP frame pass and a few primal-dual iterations
-at full size per step (ms_per_step is that sample's wall time), composed into
+back projection, one warp, one CP frame pass at full size and 50 primal-dual
+iterations at each pyramid level per step (ms_per_step is that sample's wall
+time), composed into
 outer-iter/s from the op counts of one whole outer iteration measured on the
 GPU (outer_iteration_counts_256.json in the package; the GPU path performs the
 reference's operations bit for bit, so the counts are the reference's too).
@@ -116,7 +117,9 @@ def outer_counts(args):
             d = json.load(f)
     except (OSError, ValueError):
         return None
-    return {k: float(d["op_counts"][k]) for k in COUNT_KEYS}
+    c = {k: float(d["op_counts"][k]) for k in COUNT_KEYS}
+    c["pd_iterations_per_level"] = [float(x) for x in d["pd_iterations_per_level_finest_first"]]
+    return c
 
 
 def bench_config(args, F):
@@ -237,9 +240,26 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu), for the CPU legs' reports."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_sample(args, counts, threads):
     """Time the oracle port of the reference's CPU path on a bounded sample and
-    compose seconds per outer iteration from the GPU run's op counts."""
+    compose seconds per outer iteration from the op counts of one outer
+    iteration: one forward projection, one bicubic backprojection, one warp
+    (on 4 threads, the reference's hard-coded worker count, advection.h:134-141),
+    one CP frame pass, and 50 primal-dual iterations (one of them a residual
+    iteration) at every pyramid level, weighted by that level's iterations."""
     import oracle as O
     import phantoms as P
     orc = O.Oracle()
@@ -260,7 +280,7 @@ def cpu_sample(args, counts, threads):
     flow = P.rbf_flow(n, amp=3.0, seed=1)
     aabb = [0, n, 0, n, 0, n]
     t0 = time.time()
-    orc.advect([n] * 3, aabb, flow, vol, 0.5, threads)
+    orc.advect([n] * 3, aabb, flow, vol, 0.5, 4)
     t["advect"] = time.time() - t0
     nv = n ** 3
     ytv = np.zeros((3, n, n, n), np.float32)
@@ -272,18 +292,26 @@ def cpu_sample(args, counts, threads):
     orc.lib.orc_cp_primal(O.ctypes.byref(scan), box, 1, ytp.ctypes.data, ytp, ytv, v2, xp)
     orc.lib.orc_cp_overrelax(np.array([n] * 3, np.int32), box, v2, xp, ytp)
     t["cp"] = time.time() - t0
-    V = np.zeros((3, n, n, n), np.float32)
-    Y = [np.zeros((3, n, n, n), np.float32) for _ in range(3)] + [np.zeros((n, n, n), np.float32)]
-    roi = [8] * 6
-    pd_its = 4
-    orc.flow_level([n] * 3, vol, v2, V, *Y, 0.0, 0.05, pd_its - 1, 1, aabb, roi, deterministic=0)
-    t["pd_voxel_iter"] = orc.lib.orc_last_pd_seconds() / pd_its / nv
+    del ytv, ytp, xp
+    pd_its = 50
+    t["pd_iteration_per_level"] = []
+    for lev in range(len(counts["pd_iterations_per_level"])):
+        step = 1 << lev
+        m = n // step
+        I1 = np.ascontiguousarray(vol[::step, ::step, ::step])
+        I2 = np.ascontiguousarray(v2[::step, ::step, ::step])
+        V = np.zeros((3, m, m, m), np.float32)
+        Y = [np.zeros((3, m, m, m), np.float32) for _ in range(3)] + [np.zeros((m, m, m), np.float32)]
+        orc.flow_level([m] * 3, I1, I2, V, *Y, 0.0, 0.05, pd_its - 1, 1, [0, m, 0, m, 0, m],
+                       [max(1, 8 >> lev)] * 6, deterministic=0)
+        t["pd_iteration_per_level"].append(orc.lib.orc_last_pd_seconds() / pd_its)
     sec = (counts["projections"] * t["fp"] + counts["backprojections"] * t["bp"] +
            counts["advect_voxels"] / nv * t["advect"] + counts["cp_frame_passes"] * t["cp"] +
-           counts["pd_voxel_iters"] * t["pd_voxel_iter"])
-    sample = ("composed from one %d^3->%d^2 forward projection, one bicubic backprojection, one warp, one CP "
-              "frame pass and %d timed primal-dual iterations at %d^3 (OpenMP, all host cores), weighted by the op "
-              "counts of one outer iteration" % (n, args.det, pd_its, n))
+           sum(i * s for i, s in zip(counts["pd_iterations_per_level"], t["pd_iteration_per_level"])))
+    sample = ("composed from one %d^3->%d^2 forward projection, one bicubic backprojection, one warp (4 threads, "
+              "as the reference), one CP frame pass and %d primal-dual iterations at each of %d pyramid levels "
+              "(OpenMP, %d threads; CPU: %s), weighted by the op counts of one outer iteration"
+              % (n, d, pd_its, len(counts["pd_iterations_per_level"]), threads, cpu_model()))
     return sec, t, sample
 
 
@@ -566,6 +594,7 @@ def run_gb300(args):
         source = "measured counts of one whole outer iteration (%s)" % os.path.relpath(OUTER_COUNTS, REPO)
         if counts is None:
             counts = {k: agg[k] * F / K for k in COUNT_KEYS}
+            counts["pd_iterations_per_level"] = [x * F / K for x in lev_its]
             source = "counts of the timed frame-steps, times frames / steps"
         threads = os.cpu_count() or 1
         w0 = time.time()
@@ -618,7 +647,8 @@ def run_reference(args):
                   "backprojections": float(5 * 2 * win.sum() + win.sum()),
                   "advect_voxels": float(2 * win.sum() * nv + (F - 1) * 3 * lvl * nv),
                   "cp_frame_passes": float(5 * F),
-                  "pd_voxel_iters": float((F - 1) * 3 * (args.flow_iters + 1) * lvl * nv)}
+                  "pd_voxel_iters": float((F - 1) * 3 * (args.flow_iters + 1) * lvl * nv),
+                  "pd_iterations_per_level": [float((F - 1) * 3 * (args.flow_iters + 1))] * args.scales}
         source = "op counts from the schedule's structure, every flow level at its iteration cap"
     threads = os.cpu_count() or 1
     composed, walls, parts = [], [], None
