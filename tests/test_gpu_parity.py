@@ -508,6 +508,34 @@ def test_precision_form_fp16_flow_state(setup, orc, wapmod):
         ctx.set_tuning("flow_bits", 32)
 
 
+def test_precision_form_stops_like_fp32(setup, orc, wapmod):
+    """With the reference's tolerance (0.008) the precision form's flow level
+    stops before its iteration cap as the exact FP32 path does, at a nearby
+    iteration: its residual compares the stored FP16 states (the dual sees the
+    new flow as stored), so FP16 rounding alone does not hold it above the
+    tolerance."""
+    s = setup
+    torch, ctx = s["torch"], s["ctx"]
+    aabb, I1, I2 = _flow_inputs(s, orc)
+    V0 = (s["flow"] * 0.3).astype(np.float32)
+    cap = 3000
+    its = {}
+    try:
+        for bits in (32, 16):
+            ctx.set_tuning("flow_bits", bits)
+            dV = dev(torch, V0)
+            dY = [torch.zeros((3, N, N, N), device="cuda") for _ in range(3)] + [torch.zeros((N, N, N), device="cuda")]
+            its[bits] = list(ctx.flow_level([N] * 3, dev(torch, I1), dev(torch, I2), dV, *dY, 0.008, 0.05, cap, 2,
+                                            aabb, [4] * 6))
+    finally:
+        ctx.set_tuning("flow_bits", 32)
+    print("iterations per warp: FP32", its[32], "FP16", its[16])
+    for w in range(2):
+        assert its[32][w] < cap, its
+        assert its[16][w] < cap, its
+        assert abs(its[16][w] - its[32][w]) <= max(100, its[32][w] // 4), its
+
+
 def test_precision_form_projector(setup, orc):
     """The precision form's SART step: the forward projector reads an FP16
     brick-layout copy of the volume and sums each ray with Kahan's
