@@ -47,7 +47,9 @@ WAP_API int wap_analyze_save(const char *path, const float *h_data, const int *d
  * NULL).  Read: classic little- or big-endian TIFF, strips or tiles, one
  * sample per pixel of 8/16/32/64 bits, no compression, PackBits, LZW or
  * Deflate (through the system's zlib), horizontal-differencing predictor;
- * anything else, and any malformed file, is WAP_EIO. */
+ * anything else, and any malformed file, is WAP_EIO.  Pages wider or taller
+ * than 2^20 pixels, or stacks of more than 2^33 samples, are WAP_ETOOBIG; a
+ * failed host allocation is WAP_ENOMEM. */
 WAP_API int wap_tiff_info(const char *path, int *dims4, int *bits, int *sample_format);
 /* Loads all pages, page after page (x fastest), into h_out (count >= W*H*pages floats). */
 WAP_API int wap_tiff_load(const char *path, float *h_out, size_t count);

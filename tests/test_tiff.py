@@ -234,3 +234,25 @@ def test_malformed_files_are_refused(wapmod, tmp_path):
             wapmod.tiff_load(q)
     with pytest.raises(wapmod.WapError):
         wapmod.tiff_load(str(tmp_path / "missing.tif"))
+
+
+def test_oversized_header_is_refused_before_allocation(wapmod, tmp_path):
+    """A header that claims a page of 2^30 x 8 pixels (far more than the file
+    holds) is WAP_ETOOBIG (6) from wap_tiff_info, before any page buffer is
+    allocated."""
+    import struct
+    p = str(tmp_path / "ok.tif")
+    write_tiff(p, [np.arange(64, dtype=np.uint16).reshape(8, 8)])
+    data = bytearray(open(p, "rb").read())
+    ifd = struct.unpack_from("<I", data, 4)[0]
+    n = struct.unpack_from("<H", data, ifd)[0]
+    for i in range(n):
+        e = ifd + 2 + 12 * i
+        tag, typ = struct.unpack_from("<HH", data, e)
+        if tag == 256:  # ImageWidth, rewritten as a LONG of 2^30
+            struct.pack_into("<HHII", data, e, 256, 4, 1, 1 << 30)
+    q = str(tmp_path / "huge.tif")
+    with open(q, "wb") as f:
+        f.write(bytes(data))
+    with pytest.raises(wapmod.WapError, match="status 6"):
+        wapmod.tiff_info(q)

@@ -9,18 +9,25 @@
 // Deflate (Deflate through the system's zlib, opened at run time), with the
 // horizontal-differencing predictor.  Every offset and length read from the
 // file is checked against its size; a malformed or unsupported file is
-// WAP_EIO with no partial output.
+// WAP_EIO with no partial output.  Pages are at most kMaxSide pixels a side
+// and a stack at most kMaxSamples samples (WAP_ETOOBIG beyond), so a header
+// cannot ask for an unbounded allocation; a failed host allocation is
+// WAP_ENOMEM.
 #include <dlfcn.h>
 
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
 #include "wap/wap_io.h"
 
 namespace {
+
+constexpr uint32_t kMaxSide = 1u << 20;       // pixels per page side
+constexpr uint64_t kMaxSamples = 1ull << 33;  // samples per stack (32 GB as float)
 
 struct Ifd {
   uint32_t w = 0, h = 0, bps = 1, spp = 1, fmt = 1, comp = 1, planar = 1, pred = 1, rps = 0xffffffffu, tw = 0,
@@ -45,10 +52,9 @@ struct File {
 bool read_file(const char *path, std::vector<uint8_t> &out) {
   FILE *f = std::fopen(path, "rb");
   if (!f) return false;
-  std::fseek(f, 0, SEEK_END);
-  const long n = std::ftell(f);
-  std::fseek(f, 0, SEEK_SET);
-  bool good = n >= 8;
+  const bool seek = std::fseek(f, 0, SEEK_END) == 0;
+  const long n = seek ? std::ftell(f) : -1;
+  bool good = n >= 8 && std::fseek(f, 0, SEEK_SET) == 0;
   if (good) {
     out.resize((size_t)n);
     good = std::fread(out.data(), 1, (size_t)n, f) == (size_t)n;
@@ -325,12 +331,13 @@ int open_tiff(const char *path, File &F, std::vector<Ifd> &ifds) {
   const Ifd &d0 = ifds[0];
   for (const Ifd &d : ifds)
     if (d.w != d0.w || d.h != d0.h || d.w == 0 || d.h == 0) return WAP_EIO;
+  if (d0.w > kMaxSide || d0.h > kMaxSide || (uint64_t)d0.w * d0.h * ifds.size() > kMaxSamples) return WAP_ETOOBIG;
   return WAP_OK;
 }
 
 }  // namespace
 
-extern "C" int wap_tiff_info(const char *path, int *dims4, int *bits, int *sample_format) {
+extern "C" int wap_tiff_info(const char *path, int *dims4, int *bits, int *sample_format) try {
   File F;
   std::vector<Ifd> ifds;
   const int rc = open_tiff(path, F, ifds);
@@ -344,9 +351,11 @@ extern "C" int wap_tiff_info(const char *path, int *dims4, int *bits, int *sampl
   if (bits) *bits = (int)ifds[0].bps;
   if (sample_format) *sample_format = (int)ifds[0].fmt;
   return WAP_OK;
+} catch (const std::bad_alloc &) {
+  return WAP_ENOMEM;
 }
 
-extern "C" int wap_tiff_load(const char *path, float *h_out, size_t count) {
+extern "C" int wap_tiff_load(const char *path, float *h_out, size_t count) try {
   File F;
   std::vector<Ifd> ifds;
   const int rc = open_tiff(path, F, ifds);
@@ -359,4 +368,6 @@ extern "C" int wap_tiff_load(const char *path, float *h_out, size_t count) {
     if (!load_page(F, ifds[z], tmp.data() + z * page, why)) return WAP_EIO;
   std::memcpy(h_out, tmp.data(), tmp.size() * sizeof(float));
   return WAP_OK;
+} catch (const std::bad_alloc &) {
+  return WAP_ENOMEM;
 }
