@@ -28,11 +28,12 @@ extern "C" {
 enum {
   WAP_OK = 0,
   WAP_EINVAL = 1,   /* bad argument or size */
-  WAP_ENOMEM = 2,   /* device allocation failed */
+  WAP_ENOMEM = 2,   /* device or host allocation failed */
   WAP_ECUDA = 3,    /* CUDA runtime error */
   WAP_ESTATE = 4,   /* call out of order (e.g. no level set up) */
   WAP_ENODEV = 5,   /* no usable GPU */
-  WAP_ETOOBIG = 6   /* problem larger than a fixed-capacity entry point allows */
+  WAP_ETOOBIG = 6,  /* problem larger than a fixed-capacity entry point allows */
+  WAP_EHOST = 8     /* other host-side failure (e.g. a worker thread could not start); 7 is WAP_EIO */
 };
 
 typedef struct wap_ctx wap_ctx;

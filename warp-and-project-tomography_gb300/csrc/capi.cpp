@@ -21,6 +21,7 @@
 #include <tuple>
 #include <vector>
 
+#include "c_boundary.h"
 #include "wap/wap.h"
 #include "wap/wap_serve.h"
 #include "wap_flow.h"
@@ -1209,7 +1210,7 @@ size_t flow_pairs_bytes(const int vol[3], int flow_scales, float flow_eta) {
 
 extern "C" {
 
-int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_deg, int device) {
+int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_deg, int device) try {
   if (!out || !scan || !h_angles_deg) return WAP_EINVAL;
   *out = nullptr;
   for (int a = 0; a < 3; ++a)
@@ -1249,9 +1250,9 @@ int wap_create(wap_ctx **out, const wap_scan_desc *scan, const double *h_angles_
   CU(cudaStreamSynchronize(ctx->stream));
   *out = c.release();
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_create_compute(wap_ctx **out, int device) {
+int wap_create_compute(wap_ctx **out, int device) try {
   if (!out) return WAP_EINVAL;
   *out = nullptr;
   int ndev = 0;
@@ -1265,9 +1266,9 @@ int wap_create_compute(wap_ctx **out, int device) {
   CU(ctx->maxbits.ensure(sizeof(unsigned)));
   *out = c.release();
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_alloc(wap_ctx *ctx, size_t bytes, void **d_out) {
+int wap_alloc(wap_ctx *ctx, size_t bytes, void **d_out) try {
   CHECK(ctx && d_out, WAP_EINVAL, "null argument");
   *d_out = nullptr;
   CU(cudaSetDevice(ctx->device));
@@ -1277,43 +1278,43 @@ int wap_alloc(wap_ctx *ctx, size_t bytes, void **d_out) {
     return fail(ctx, WAP_ENOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
   }
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_free(wap_ctx *ctx, void *d_ptr) {
+int wap_free(wap_ctx *ctx, void *d_ptr) try {
   CHECK(ctx, WAP_EINVAL, "null context");
   if (d_ptr) {
     CU(cudaStreamSynchronize(ctx->stream));
     CU(cudaFree(d_ptr));
   }
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_copy_to_device(wap_ctx *ctx, void *d_dst, const void *h_src, size_t bytes) {
+int wap_copy_to_device(wap_ctx *ctx, void *d_dst, const void *h_src, size_t bytes) try {
   CHECK(ctx && (bytes == 0 || (d_dst && h_src)), WAP_EINVAL, "null argument");
   if (bytes) CU(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_copy_to_host(wap_ctx *ctx, void *h_dst, const void *d_src, size_t bytes) {
+int wap_copy_to_host(wap_ctx *ctx, void *h_dst, const void *d_src, size_t bytes) try {
   CHECK(ctx && (bytes == 0 || (h_dst && d_src)), WAP_EINVAL, "null argument");
   if (bytes) CU(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_fill_zero(wap_ctx *ctx, void *d_ptr, size_t bytes) {
+int wap_fill_zero(wap_ctx *ctx, void *d_ptr, size_t bytes) try {
   CHECK(ctx && (bytes == 0 || d_ptr), WAP_EINVAL, "null argument");
   if (bytes) CU(cudaMemsetAsync(d_ptr, 0, bytes, ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user) {
+int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user) try {
   CHECK(ctx, WAP_EINVAL, "null context");
   ctx->observer = fn;
   ctx->observer_user = user;
   return WAP_OK;
-}
+} WAP_CATCH
 
 void wap_destroy(wap_ctx *ctx) {
   if (!ctx) return;
@@ -1336,7 +1337,7 @@ size_t wap_trim_cache(int device) { return cache_trim(device); }
 
 const char *wap_last_error(const wap_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-int wap_set_stream(wap_ctx *ctx, void *cuda_stream) {
+int wap_set_stream(wap_ctx *ctx, void *cuda_stream) try {
   CHECK(ctx, WAP_EINVAL, "null context");
   if (ctx->own_stream && ctx->stream) {
     CU(cudaStreamSynchronize(ctx->stream));
@@ -1345,21 +1346,21 @@ int wap_set_stream(wap_ctx *ctx, void *cuda_stream) {
   ctx->stream = (cudaStream_t)cuda_stream;
   ctx->own_stream = false;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_synchronize(wap_ctx *ctx) {
+int wap_synchronize(wap_ctx *ctx) try {
   CHECK(ctx, WAP_EINVAL, "null context");
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_get_stats(wap_ctx *ctx, wap_stats *out) {
+int wap_get_stats(wap_ctx *ctx, wap_stats *out) try {
   CHECK(ctx && out, WAP_EINVAL, "null argument");
   *out = ctx->stats;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_set_profiling(wap_ctx *ctx, int on) {
+int wap_set_profiling(wap_ctx *ctx, int on) try {
   CHECK(ctx, WAP_EINVAL, "null context");
   ctx->profiling = on ? 1 : 0;
   if (ctx->profiling && ctx->pd_events.empty()) {
@@ -1367,9 +1368,9 @@ int wap_set_profiling(wap_ctx *ctx, int on) {
     for (auto &e : ctx->pd_events) CU(cudaEventCreate(&e));
   }
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
+int wap_set_tuning(wap_ctx *ctx, const char *key, int value) try {
   CHECK(ctx && key, WAP_EINVAL, "null argument");
   const std::string k = key;
   if (k == "pd_form") {
@@ -1400,18 +1401,18 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) {
   ctx->pd_plans.clear();
   ctx->pd_plans16.clear();
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_get_tuning(wap_ctx *ctx, const int *dims, int *h_form, int *h_zchunk) {
+int wap_get_tuning(wap_ctx *ctx, const int *dims, int *h_form, int *h_zchunk) try {
   CHECK(ctx && dims && h_form && h_zchunk, WAP_EINVAL, "null argument");
   const auto &plans = ctx->flow_bits == 16 ? ctx->pd_plans16 : ctx->pd_plans;  // the current precision's plans
   auto it = plans.find(std::make_tuple(dims[0], dims[1], dims[2]));
   *h_form = it == plans.end() ? ctx->pd_form : it->second.first;
   *h_zchunk = it == plans.end() ? ctx->pd_zchunk : it->second.second;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_upload_projections(wap_ctx *ctx, const float *h_projs) {
+int wap_upload_projections(wap_ctx *ctx, const float *h_projs) try {
   CHECK(ctx && h_projs, WAP_EINVAL, "null argument");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   const size_t n = ctx->np * ctx->scan.nproj;
@@ -1424,9 +1425,9 @@ int wap_upload_projections(wap_ctx *ctx, const float *h_projs) {
   ctx->gmax = m;
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_set_projections_device(wap_ctx *ctx, const float *d_projs) {
+int wap_set_projections_device(wap_ctx *ctx, const float *d_projs) try {
   CHECK(ctx && d_projs, WAP_EINVAL, "null argument");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   ctx->projs = d_projs;
@@ -1436,18 +1437,18 @@ int wap_set_projections_device(wap_ctx *ctx, const float *d_projs) {
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->gmax = decode_max_bits(bits);
   return WAP_OK;
-}
+} WAP_CATCH
 
 float wap_gmax(const wap_ctx *ctx) { return ctx ? ctx->gmax : 0.0f; }
 
-int wap_set_gmax(wap_ctx *ctx, float gmax) {
+int wap_set_gmax(wap_ctx *ctx, float gmax) try {
   CHECK(ctx, WAP_EINVAL, "null context");
   ctx->gmax = gmax;
   return WAP_OK;
-}
+} WAP_CATCH
 
 int wap_projection_geometry(const wap_scan_desc *scan, double angle_deg, float *h_p2m, float *h_m2v, float *h_mvv2m,
-                            float *h_eye) {
+                            float *h_eye) try {
   if (!scan || !h_p2m || !h_m2v || !h_mvv2m || !h_eye) return WAP_EINVAL;
   ScanGeometry sg{};
   for (int a = 0; a < 3; ++a) sg.vol[a] = scan->vol[a];
@@ -1464,14 +1465,14 @@ int wap_projection_geometry(const wap_scan_desc *scan, double angle_deg, float *
   std::memcpy(h_mvv2m, g.mvv2m, sizeof(g.mvv2m));
   std::memcpy(h_eye, g.eye, sizeof(g.eye));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_level_frames(const wap_scan_desc *scan, int level, int *start, int *end, float *ftime, float *tunit, int cap) {
+int wap_level_frames(const wap_scan_desc *scan, int level, int *start, int *end, float *ftime, float *tunit, int cap) try {
   if (!scan || level < 0 || level > 4) return -WAP_EINVAL;
   return level_frames(scan->nframes_cli, scan->nproj, level, start, end, ftime, tunit, cap);
-}
+} WAP_CATCH
 
-int wap_level_setup(wap_ctx *ctx, int level) {
+int wap_level_setup(wap_ctx *ctx, int level) try {
   CHECK(ctx, WAP_EINVAL, "null context");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(level >= 0 && level <= 4, WAP_EINVAL, "level out of range");
@@ -1501,43 +1502,43 @@ int wap_level_setup(wap_ctx *ctx, int level) {
   TRY(ensure_level_buffers(ctx));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
 int wap_level_nframes(const wap_ctx *ctx) { return ctx ? ctx->F : 0; }
 
-int wap_frame_volume_upload(wap_ctx *ctx, int frame, const float *h_vol) {
+int wap_frame_volume_upload(wap_ctx *ctx, int frame, const float *h_vol) try {
   CHECK(ctx && h_vol, WAP_EINVAL, "null argument");
   CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
   CU(cudaMemcpyAsync(vol_ptr(ctx, frame), h_vol, sizeof(float) * ctx->nv, cudaMemcpyHostToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_frame_volume_download(wap_ctx *ctx, int frame, float *h_vol) {
+int wap_frame_volume_download(wap_ctx *ctx, int frame, float *h_vol) try {
   CHECK(ctx && h_vol, WAP_EINVAL, "null argument");
   CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
   CU(cudaMemcpyAsync(h_vol, vol_ptr(ctx, frame), sizeof(float) * ctx->nv, cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_frame_flow_upload(wap_ctx *ctx, int frame, const float *h_flow) {
+int wap_frame_flow_upload(wap_ctx *ctx, int frame, const float *h_flow) try {
   CHECK(ctx && h_flow, WAP_EINVAL, "null argument");
   CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
   CU(cudaMemcpyAsync(flow_ptr(ctx, frame), h_flow, sizeof(float) * 3 * ctx->nv, cudaMemcpyHostToDevice,
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_frame_flow_download(wap_ctx *ctx, int frame, float *h_flow) {
+int wap_frame_flow_download(wap_ctx *ctx, int frame, float *h_flow) try {
   CHECK(ctx && h_flow, WAP_EINVAL, "null argument");
   CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
   CU(cudaMemcpyAsync(h_flow, flow_ptr(ctx, frame), sizeof(float) * 3 * ctx->nv, cudaMemcpyDeviceToHost,
                      ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
 float *wap_frame_volume_device(wap_ctx *ctx, int frame) {
   if (!ctx || frame < 0 || frame >= ctx->F) return nullptr;
@@ -1549,7 +1550,7 @@ float *wap_frame_flow_device(wap_ctx *ctx, int frame) {
   return flow_ptr(ctx, frame);
 }
 
-int wap_level_advance(wap_ctx *ctx) {
+int wap_level_advance(wap_ctx *ctx) try {
   CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
   const int F0 = ctx->F;
   const size_t nv = ctx->nv;
@@ -1564,14 +1565,14 @@ int wap_level_advance(wap_ctx *ctx) {
                            cudaMemcpyDeviceToDevice, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_forward_project(wap_ctx *ctx, int proj, const float *d_vol, float *d_img, float *d_len, float *d_weight) {
+int wap_forward_project(wap_ctx *ctx, int proj, const float *d_vol, float *d_img, float *d_len, float *d_weight) try {
   return wap_forward_project_batch(ctx, 1, &proj, &d_vol, &d_img, &d_len, &d_weight);
-}
+} WAP_CATCH
 
 int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const float *const *h_d_vols,
-                              float *const *h_d_imgs, float *const *h_d_lens, float *const *h_d_weights) {
+                              float *const *h_d_imgs, float *const *h_d_lens, float *const *h_d_weights) try {
   CHECK(ctx && h_proj && h_d_vols, WAP_EINVAL, "null argument");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(njobs >= 1 && njobs <= 65535, WAP_EINVAL, "job count out of range");
@@ -1599,18 +1600,18 @@ int wap_forward_project_batch(wap_ctx *ctx, int njobs, const int *h_proj, const 
                     ctx->scan.det[1], ctx->sd, ctx->scan.alpha, ctx->stream, bricks));
   ctx->stats.fp_launches++;
   return WAP_OK;
-}
+} WAP_CATCH
 
 int wap_correction(wap_ctx *ctx, int n, const float *d_meas, const float *d_img, const float *d_len, float *d_dual,
-                   float *d_corr) {
+                   float *d_corr) try {
   CHECK(ctx && d_meas && d_img && d_len && d_corr, WAP_EINVAL, "null argument");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   KL(launch_correction(n, d_meas, d_img, d_len, d_dual, ctx->scan.alpha, d_corr, ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
 int wap_backproject_voxel(wap_ctx *ctx, int proj, const float *d_corr, const int *box, int mode, int exact,
-                          float *d_vol) {
+                          float *d_vol) try {
   CHECK(ctx && d_corr && box && d_vol, WAP_EINVAL, "null argument");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(proj >= 0 && proj < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
@@ -1630,9 +1631,9 @@ int wap_backproject_voxel(wap_ctx *ctx, int proj, const float *d_corr, const int
                      ctx->scan.det[1], ctx->halfW, ctx->halfH, (float)ctx->scan.sdd, ctx->scan.ds, ctx->scan.alpha,
                      ctx->gmax, mode, exact, ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_contrib, float *d_weight) {
+int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_contrib, float *d_weight) try {
   CHECK(ctx && d_corr && d_contrib && d_weight, WAP_EINVAL, "null argument");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(proj >= 0 && proj < ctx->scan.nproj, WAP_EINVAL, "projection index out of range");
@@ -1641,10 +1642,10 @@ int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, float *d_co
   KL(launch_ray_splat(ctx->geom.as<ProjGeom>(), ctx->jobs_misc.as<SplatJob>(), 1, ctx->scan.vol, ctx->scan.det[0],
                       ctx->scan.det[1], ctx->sd, ctx->stream, ctx->splat_direct != 0));
   return WAP_OK;
-}
+} WAP_CATCH
 
 int wap_advect(wap_ctx *ctx, const int *dims, const float *aabb, const float *d_vel, const float *d_src, int nc,
-               float dt, float *d_out) {
+               float dt, float *d_out) try {
   CHECK(ctx && dims && aabb && d_vel && d_src && d_out, WAP_EINVAL, "null argument");
   CHECK(dims[0] >= 3 && dims[1] >= 3 && dims[2] >= 3 && nc >= 1, WAP_EINVAL, "grid must be at least 3^3");
   CHECK(aabb[1] > aabb[0] && aabb[3] > aabb[2] && aabb[5] > aabb[4], WAP_EINVAL, "empty bounding box");
@@ -1658,22 +1659,22 @@ int wap_advect(wap_ctx *ctx, const int *dims, const float *aabb, const float *d_
                    ctx->adv_flags.as<int>()));
   CU(cudaStreamSynchronize(ctx->stream));  // the host table and job list are reused by the next call
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_blur(wap_ctx *ctx, const int *dims, int nc, float sigma, const float *d_src, float *d_out) {
+int wap_blur(wap_ctx *ctx, const int *dims, int nc, float sigma, const float *d_src, float *d_out) try {
   CHECK(ctx && dims && d_src && d_out, WAP_EINVAL, "null argument");
   return do_blur(ctx, dims, nc, sigma, d_src, d_out);
-}
+} WAP_CATCH
 
-int wap_resize(wap_ctx *ctx, const int *dims, int nc, const float *d_src, const int *odims, float *d_out) {
+int wap_resize(wap_ctx *ctx, const int *dims, int nc, const float *d_src, const int *odims, float *d_out) try {
   CHECK(ctx && dims && odims && d_src && d_out, WAP_EINVAL, "null argument");
   for (int a = 0; a < 3; ++a) CHECK(dims[a] >= 1 && odims[a] >= 1, WAP_EINVAL, "empty grid");
   return do_resize(ctx, dims, nc, d_src, odims, d_out);
-}
+} WAP_CATCH
 
 int wap_flow_level(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, float *d_V, float *d_Y1,
                    float *d_Y2, float *d_Y3, float *d_Y4, float tol, float lambda, int max_iters, int nwarps,
-                   const float *aabb, const int *roi6, int *h_iters) {
+                   const float *aabb, const int *roi6, int *h_iters) try {
   CHECK(ctx && dims && d_I1 && d_I2 && d_V && d_Y1 && d_Y2 && d_Y3 && d_Y4 && aabb && roi6, WAP_EINVAL,
         "null argument");
   CHECK(dims[0] >= 3 && dims[1] >= 3 && dims[2] >= 3, WAP_EINVAL, "grid must be at least 3^3");
@@ -1681,23 +1682,23 @@ int wap_flow_level(wap_ctx *ctx, const int *dims, const float *d_I1, const float
   TRY(flow_level(ctx, dims, d_I1, d_I2, d_V, Y, tol, lambda, max_iters, nwarps, aabb, roi6, h_iters, nullptr));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
 int wap_flow_multiscale(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, const float *d_V0,
                         float tol, float lambda, int max_iters, int nwarps, float eta, float sigma, int scales,
-                        const int *cut6, float *d_Vout, long long *h_total_iters) {
+                        const int *cut6, float *d_Vout, long long *h_total_iters) try {
   CHECK(ctx && dims && d_I1 && d_I2 && d_V0 && cut6 && d_Vout, WAP_EINVAL, "null argument");
   long long tot = 0;
   TRY(flow_multiscale(ctx, dims, d_I1, d_I2, d_V0, tol, lambda, max_iters, nwarps, eta, sigma, scales, cut6, d_Vout,
                       &tot));
   if (h_total_iters) *h_total_iters = tot;
   return WAP_OK;
-}
+} WAP_CATCH
 
 int wap_flow_multiscale_warm(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, const float *d_V0,
                              const float *d_Y1, const float *d_Y2, const float *d_Y3, const float *d_Y4, float tol,
                              float lambda, int max_iters, int nwarps, float eta, float sigma, int scales,
-                             const int *cut6, float *d_Vout, long long *h_total_iters) {
+                             const int *cut6, float *d_Vout, long long *h_total_iters) try {
   CHECK(ctx && dims && d_I1 && d_I2 && d_V0 && cut6 && d_Vout, WAP_EINVAL, "null argument");
   CHECK((d_Y1 && d_Y2 && d_Y3 && d_Y4) || (!d_Y1 && !d_Y2 && !d_Y3 && !d_Y4), WAP_EINVAL,
         "give all four dual fields or none");
@@ -1707,9 +1708,9 @@ int wap_flow_multiscale_warm(wap_ctx *ctx, const int *dims, const float *d_I1, c
                       &tot, d_Y1 ? Y0 : nullptr));
   if (h_total_iters) *h_total_iters = tot;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_sart_prox(wap_ctx *ctx, int frame, int nb_sart, int cut, int exact) {
+int wap_sart_prox(wap_ctx *ctx, int frame, int nb_sart, int cut, int exact) try {
   CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
   CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
   CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
@@ -1719,9 +1720,9 @@ int wap_sart_prox(wap_ctx *ctx, int frame, int nb_sart, int cut, int exact) {
   TRY(sart_frames(ctx, frames, nb_sart, box, exact));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exact) {
+int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exact) try {
   CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
   CHECK(ctx->projs, WAP_ESTATE, "no projections uploaded");
   CHECK(frame >= 0 && frame < ctx->F, WAP_EINVAL, "frame out of range");
@@ -1730,9 +1731,9 @@ int wap_warp_and_project(wap_ctx *ctx, int frame, int proj, float rtime, int exa
   TRY(wap_step(ctx, items, exact));
   CU(cudaStreamSynchronize(ctx->stream));
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_adaptive_warp(wap_ctx *ctx, int frame, int nb_warp, int cut, int exact) {
+int wap_adaptive_warp(wap_ctx *ctx, int frame, int nb_warp, int cut, int exact) try {
   CHECK(ctx, WAP_EINVAL, "null argument");
   CHECK(has_scan(ctx), WAP_ESTATE, "context has no scan (wap_create_compute)");
   CHECK(ctx->level >= 0, WAP_ESTATE, "no level set up");
@@ -1741,9 +1742,9 @@ int wap_adaptive_warp(wap_ctx *ctx, int frame, int nb_warp, int cut, int exact) 
   CHECK(cut >= 0 && 2 * cut < ctx->scan.vol[0] && 2 * cut < ctx->scan.vol[1] && 2 * cut < ctx->scan.vol[2], WAP_EINVAL,
         "cut must leave a non-empty ROI");
   return adaptive_warp(ctx, frame, nb_warp, cut, exact);
-}
+} WAP_CATCH
 
-int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1, wap_stats *stats) {
+int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1, wap_stats *stats) try {
   TRY(check_schedule(ctx, sch, f0, f1));
   ctx->stats = wap_stats{};
   cudaEvent_t ev[4];
@@ -1767,14 +1768,14 @@ int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, in
   ctx->stats.ms_wap = ms[2];
   if (stats) *stats = ctx->stats;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_outer_iteration_nsteps(const wap_ctx *ctx, const wap_schedule *sch) {
+int wap_outer_iteration_nsteps(const wap_ctx *ctx, const wap_schedule *sch) try {
   if (!ctx || !sch || ctx->level < 0) return -1;
   return sch->n_cp + std::max(ctx->F - 1, 0) + 1;
-}
+} WAP_CATCH
 
-int wap_outer_iteration_step(wap_ctx *ctx, const wap_schedule *sch, int step, wap_stats *stats) {
+int wap_outer_iteration_step(wap_ctx *ctx, const wap_schedule *sch, int step, wap_stats *stats) try {
   TRY(check_schedule(ctx, sch, 0, ctx ? ctx->F : 0));
   const int nflow = std::max(ctx->F - 1, 0);
   CHECK(step >= 0 && step < sch->n_cp + nflow + 1, WAP_EINVAL, "step out of range");
@@ -1802,7 +1803,7 @@ int wap_outer_iteration_step(wap_ctx *ctx, const wap_schedule *sch, int step, wa
   (phase == 0 ? ctx->stats.ms_cp : phase == 1 ? ctx->stats.ms_flow : ctx->stats.ms_wap) = ms;
   if (stats) *stats = ctx->stats;
   return WAP_OK;
-}
+} WAP_CATCH
 
 size_t wap_ctx_device_bytes(const wap_ctx *ctx) {
   if (!ctx) return 0;
@@ -1858,10 +1859,10 @@ size_t wap_job_device_bytes(const wap_scan_desc *scan, const wap_schedule *sch) 
   return floats * sizeof(float) + tables;
 }
 
-int wap_outer_iteration(wap_ctx *ctx, const wap_schedule *sch, wap_stats *stats) {
+int wap_outer_iteration(wap_ctx *ctx, const wap_schedule *sch, wap_stats *stats) try {
   CHECK(ctx && ctx->level >= 0, WAP_ESTATE, "no level set up");
   return wap_outer_iteration_frames(ctx, sch, 0, ctx->F, stats);
-}
+} WAP_CATCH
 
 }  // extern "C"
 
@@ -2128,7 +2129,7 @@ cudaError_t stream_follow(cudaStream_t dst, cudaStream_t src) {
 
 extern "C" {
 
-int wap_batch_create(wap_batch **out, wap_ctx *const *ctxs, int n) {
+int wap_batch_create(wap_batch **out, wap_ctx *const *ctxs, int n) try {
   if (!out || !ctxs || n < 1) return WAP_EINVAL;
   *out = nullptr;
   std::unique_ptr<wap_batch> b(new wap_batch);
@@ -2145,7 +2146,7 @@ int wap_batch_create(wap_batch **out, wap_ctx *const *ctxs, int n) {
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) return WAP_ECUDA;
   *out = b.release();
   return WAP_OK;
-}
+} WAP_CATCH
 
 void wap_batch_destroy(wap_batch *b) {
   if (!b) return;
@@ -2158,21 +2159,21 @@ void wap_batch_destroy(wap_batch *b) {
 
 const char *wap_batch_last_error(const wap_batch *b) { return b ? b->err.c_str() : "null batch"; }
 
-int wap_batch_set_tuning(wap_batch *b, int fp_shape, int bp_shape) {
+int wap_batch_set_tuning(wap_batch *b, int fp_shape, int bp_shape) try {
   if (!b || fp_shape < -1 || fp_shape >= kFpShapes || bp_shape < -1 || bp_shape >= kBpShapes) return WAP_EINVAL;
   b->fp_shape = fp_shape;
   b->bp_shape = bp_shape;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_batch_get_tuning(const wap_batch *b, int *h_fp_shape, int *h_bp_shape) {
+int wap_batch_get_tuning(const wap_batch *b, int *h_fp_shape, int *h_bp_shape) try {
   if (!b || !h_fp_shape || !h_bp_shape) return WAP_EINVAL;
   *h_fp_shape = b->fp_shape;
   *h_bp_shape = b->bp_shape;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_batch_outer_iteration(wap_batch *b, const wap_schedule *scheds, wap_stats *stats) {
+int wap_batch_outer_iteration(wap_batch *b, const wap_schedule *scheds, wap_stats *stats) try {
   if (!b || !scheds) return WAP_EINVAL;
   const int n = (int)b->ctxs.size();
   for (int c = 0; c < n; ++c) {
@@ -2260,6 +2261,6 @@ int wap_batch_outer_iteration(wap_batch *b, const wap_schedule *scheds, wap_stat
     *stats = s;
   }
   return WAP_OK;
-}
+} WAP_CATCH
 
 }  // extern "C"

@@ -12,6 +12,7 @@
 // which the allocating and the allocation-free entry points below share.
 #include <cmath>
 
+#include "c_boundary.h"
 #include "wap/wap.h"
 #include "wap_internal.h"
 
@@ -193,7 +194,7 @@ using namespace wap;
 
 extern "C" int wap_cg_screened_laplacian(wap_ctx *ctx, const int *dims, float a, float b, const float *d_rhs,
                                          float *d_x, float rel_tol, int max_iters, float abs_tol, int mode,
-                                         int *h_iters) {
+                                         int *h_iters) try {
   if (!ctx || !cg_args_ok(dims, d_rhs, d_x, max_iters)) return WAP_EINVAL;
   cudaStream_t st = ctx_stream(ctx);
   const size_t n = (size_t)dims[0] * dims[1] * dims[2];
@@ -214,7 +215,7 @@ extern "C" int wap_cg_screened_laplacian(wap_ctx *ctx, const int *dims, float a,
   cudaFree(part);
   cudaFree(scal);
   return status;
-}
+} WAP_CATCH
 
 // ---------------------------------------------------------------------------
 // Allocation-free variant of wap_cg_screened_laplacian.
@@ -265,7 +266,7 @@ int noalloc_scratch(void **out) {
 
 extern "C" int wap_cg_screened_laplacian_noalloc(void *cuda_stream, const int *dims, float a, float b,
                                                  const float *d_rhs, float *d_x, float rel_tol, int max_iters,
-                                                 float abs_tol, int mode, int *h_iters) {
+                                                 float abs_tol, int mode, int *h_iters) try {
   if (h_iters) *h_iters = 0;
   if (!cg_args_ok(dims, d_rhs, d_x, max_iters)) return WAP_EINVAL;
   const size_t n = (size_t)dims[0] * dims[1] * dims[2];
@@ -282,4 +283,4 @@ extern "C" int wap_cg_screened_laplacian_noalloc(void *cuda_stream, const int *d
   // kernels), so nothing left by the previous call needs clearing.
   const CgBufs B{r, r + n, r + 2 * n, part, part + kNoAllocBlocks, scal};
   return cg_solve((cudaStream_t)cuda_stream, dims, a, b, d_rhs, d_x, rel_tol, max_iters, abs_tol, mode, B, h_iters);
-}
+} WAP_CATCH

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "wap/wap_io.h"
+#include "c_boundary.h"
 
 namespace {
 
@@ -124,7 +125,7 @@ int read_data(std::FILE *f, float *out, size_t n, bool swap, Conv conv) {
 
 extern "C" {
 
-int wap_analyze_info(const char *path, int *dims4, int *datatype) {
+int wap_analyze_info(const char *path, int *dims4, int *datatype) try {
   Header hd;
   const int r = read_header(path, hd);
   if (r != WAP_OK) return r;
@@ -132,9 +133,9 @@ int wap_analyze_info(const char *path, int *dims4, int *datatype) {
     for (int a = 0; a < 4; ++a) dims4[a] = hd.dims[a];
   if (datatype) *datatype = hd.datatype;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_analyze_load(const char *path, float *h_out, size_t count) {
+int wap_analyze_load(const char *path, float *h_out, size_t count) try {
   if (!h_out) return WAP_EINVAL;
   Header hd;
   int r = read_header(path, hd);
@@ -159,9 +160,9 @@ int wap_analyze_load(const char *path, float *h_out, size_t count) {
   }
   std::fclose(f);
   return r;
-}
+} WAP_CATCH
 
-int wap_analyze_save(const char *path, const float *h_data, const int *dims4, const float *voxel_size) {
+int wap_analyze_save(const char *path, const float *h_data, const int *dims4, const float *voxel_size) try {
   if (!path || !h_data || !dims4) return WAP_EINVAL;
   for (int a = 0; a < 4; ++a)
     if (dims4[a] < 1 || dims4[a] > 32767) return WAP_EINVAL;
@@ -208,9 +209,9 @@ int wap_analyze_save(const char *path, const float *h_data, const int *dims4, co
   ok = ok && std::fwrite(h_data, sizeof(float), n, f) == n;
   ok = (std::fclose(f) == 0) && ok;
   return ok ? WAP_OK : WAP_EIO;
-}
+} WAP_CATCH
 
-int wap_read_angles(const char *path, double *h_out, int n, int *h_read) {
+int wap_read_angles(const char *path, double *h_out, int n, int *h_read) try {
   if (!path || (!h_out && n > 0) || n < 0) return WAP_EINVAL;
   std::ifstream in(path);
   if (!in) return WAP_EIO;
@@ -220,9 +221,9 @@ int wap_read_angles(const char *path, double *h_out, int n, int *h_read) {
   for (int k = i; k < n; ++k) h_out[k] = 0.0;
   if (h_read) *h_read = i;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_split_z(int depth, int nb, int *h_first, int *h_count) {
+int wap_split_z(int depth, int nb, int *h_first, int *h_count) try {
   if (depth < 1 || nb < 1 || nb > depth || !h_first || !h_count) return WAP_EINVAL;
   if (nb == 1) {
     h_first[0] = 0;
@@ -241,9 +242,9 @@ int wap_split_z(int depth, int nb, int *h_first, int *h_count) {
     }
   }
   return k == nb ? WAP_OK : WAP_EINVAL;
-}
+} WAP_CATCH
 
-int wap_lds_angles(int np, int ns, int p, int nz, double *h_out) {
+int wap_lds_angles(int np, int ns, int p, int nz, double *h_out) try {
   if (np < 0 || ns < 1 || p < 2 || nz < 1 || (!h_out && np > 0)) return WAP_EINVAL;
   int len = 0;
   long long i = 0;
@@ -260,6 +261,6 @@ int wap_lds_angles(int np, int ns, int p, int nz, double *h_out) {
     for (int k = 0; len < np && k < ns; ++k) h_out[len++] = r + k * 360.0 / ns;
   }
   return WAP_OK;
-}
+} WAP_CATCH
 
 }  // extern "C"

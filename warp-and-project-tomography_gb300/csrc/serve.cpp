@@ -27,6 +27,7 @@
 #include "wap/wap.h"
 #include "wap/wap_serve.h"
 #include "wap_internal.h"
+#include "c_boundary.h"
 
 namespace {
 
@@ -183,7 +184,7 @@ struct wap_server {
 
 extern "C" {
 
-int wap_server_create(wap_server **out, int device, size_t hbm_budget_bytes, int workers) {
+int wap_server_create(wap_server **out, int device, size_t hbm_budget_bytes, int workers) try {
   if (!out || workers < 1 || workers > 64 || hbm_budget_bytes == 0) return WAP_EINVAL;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return WAP_ENODEV;
@@ -194,7 +195,7 @@ int wap_server_create(wap_server **out, int device, size_t hbm_budget_bytes, int
   for (int w = 0; w < workers; ++w) s->workers.emplace_back([p = s.get()] { p->worker(); });
   *out = s.release();
   return WAP_OK;
-}
+} WAP_CATCH
 
 void wap_server_destroy(wap_server *s) {
   if (!s) return;
@@ -209,7 +210,7 @@ void wap_server_destroy(wap_server *s) {
   delete s;
 }
 
-int wap_server_submit(wap_server *s, const wap_job_desc *job, long long *h_id) {
+int wap_server_submit(wap_server *s, const wap_job_desc *job, long long *h_id) try {
   if (!s || !job || !h_id || !job->h_angles || !job->h_projs || job->outer_iterations < 1) return WAP_EINVAL;
   if (job->flow_bits != 0 && job->flow_bits != 32 && job->flow_bits != 16) return WAP_EINVAL;
   const wap_scan_desc &sc = job->scan;
@@ -235,18 +236,18 @@ int wap_server_submit(wap_server *s, const wap_job_desc *job, long long *h_id) {
   s->jobs.emplace(j->id, std::move(j));
   s->cv.notify_all();
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_server_info(wap_server *s, long long id, wap_job_info *out) {
+int wap_server_info(wap_server *s, long long id, wap_job_info *out) try {
   if (!s || !out) return WAP_EINVAL;
   std::lock_guard<std::mutex> lk(s->m);
   auto it = s->jobs.find(id);
   if (it == s->jobs.end()) return WAP_EINVAL;
   *out = it->second->info;
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_server_wait(wap_server *s, long long id, double timeout_s) {
+int wap_server_wait(wap_server *s, long long id, double timeout_s) try {
   if (!s) return WAP_EINVAL;
   std::unique_lock<std::mutex> lk(s->m);
   auto it = s->jobs.find(id);
@@ -258,9 +259,9 @@ int wap_server_wait(wap_server *s, long long id, double timeout_s) {
         (j->info.state == WAP_JOB_QUEUED || j->info.state == WAP_JOB_RUNNING))
       return WAP_ESTATE;
   return j->info.state == WAP_JOB_DONE ? WAP_OK : j->info.status;
-}
+} WAP_CATCH
 
-int wap_server_result(wap_server *s, long long id, int frame, float *h_vol) {
+int wap_server_result(wap_server *s, long long id, int frame, float *h_vol) try {
   if (!s || !h_vol) return WAP_EINVAL;
   std::lock_guard<std::mutex> lk(s->m);
   auto it = s->jobs.find(id);
@@ -269,9 +270,9 @@ int wap_server_result(wap_server *s, long long id, int frame, float *h_vol) {
   if (frame < 0 || frame >= (int)j->result.size()) return WAP_EINVAL;
   std::memcpy(h_vol, j->result[frame].data(), sizeof(float) * j->result[frame].size());
   return WAP_OK;
-}
+} WAP_CATCH
 
-int wap_server_release(wap_server *s, long long id) {
+int wap_server_release(wap_server *s, long long id) try {
   if (!s) return WAP_EINVAL;
   std::lock_guard<std::mutex> lk(s->m);
   auto it = s->jobs.find(id);
@@ -280,16 +281,16 @@ int wap_server_release(wap_server *s, long long id) {
   if (st != WAP_JOB_DONE && st != WAP_JOB_FAILED) return WAP_ESTATE;
   s->jobs.erase(it);
   return WAP_OK;
-}
+} WAP_CATCH
 
 double wap_server_now(const wap_server *s) { return s ? s->now() : 0.0; }
 
-int wap_server_memory(const wap_server *s, size_t *h_in_use, size_t *h_peak) {
+int wap_server_memory(const wap_server *s, size_t *h_in_use, size_t *h_peak) try {
   if (!s) return WAP_EINVAL;
   std::lock_guard<std::mutex> lk(const_cast<wap_server *>(s)->m);
   if (h_in_use) *h_in_use = s->in_use;
   if (h_peak) *h_peak = s->peak;
   return WAP_OK;
-}
+} WAP_CATCH
 
 }  // extern "C"

@@ -12,7 +12,7 @@
 // WAP_EIO with no partial output.  Pages are at most kMaxSide pixels a side
 // and a stack at most kMaxSamples samples (WAP_ETOOBIG beyond), so a header
 // cannot ask for an unbounded allocation; a failed host allocation is
-// WAP_ENOMEM.
+// WAP_ENOMEM (WAP_CATCH).
 #include <dlfcn.h>
 
 #include <cstdint>
@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "c_boundary.h"
 #include "wap/wap_io.h"
 
 namespace {
@@ -351,9 +352,7 @@ extern "C" int wap_tiff_info(const char *path, int *dims4, int *bits, int *sampl
   if (bits) *bits = (int)ifds[0].bps;
   if (sample_format) *sample_format = (int)ifds[0].fmt;
   return WAP_OK;
-} catch (const std::bad_alloc &) {
-  return WAP_ENOMEM;
-}
+} WAP_CATCH
 
 extern "C" int wap_tiff_load(const char *path, float *h_out, size_t count) try {
   File F;
@@ -368,6 +367,4 @@ extern "C" int wap_tiff_load(const char *path, float *h_out, size_t count) try {
     if (!load_page(F, ifds[z], tmp.data() + z * page, why)) return WAP_EIO;
   std::memcpy(h_out, tmp.data(), tmp.size() * sizeof(float));
   return WAP_OK;
-} catch (const std::bad_alloc &) {
-  return WAP_ENOMEM;
-}
+} WAP_CATCH

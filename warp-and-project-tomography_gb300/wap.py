@@ -14,7 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libwap_gb300.so")
 
-WAP_OK, WAP_EINVAL, WAP_ENOMEM, WAP_ECUDA, WAP_ESTATE, WAP_ENODEV = range(6)
+WAP_OK, WAP_EINVAL, WAP_ENOMEM, WAP_ECUDA, WAP_ESTATE, WAP_ENODEV, WAP_ETOOBIG, WAP_EIO, WAP_EHOST = range(9)
 
 _c_int, _c_float, _c_double, _vp = ctypes.c_int, ctypes.c_float, ctypes.c_double, ctypes.c_void_p
 
