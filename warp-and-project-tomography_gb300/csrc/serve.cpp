@@ -70,6 +70,7 @@ struct wap_server {
   // Admission under the lock: first-fit over the queue, with the head's
   // patience rule.
   void admit_locked(std::vector<Job *> &admitted) {
+    admitted.reserve(queue.size());  // may throw; nothing has changed yet
     const double t = now();
     for (auto it = queue.begin(); it != queue.end();) {
       Job *j = *it;
@@ -129,16 +130,45 @@ struct wap_server {
     j->ctx = nullptr;
   }
 
+  // A worker's call into the library or its own host allocations: an
+  // exception (host memory) becomes the job's failure status, so it never
+  // leaves the worker thread.
+  template <class Fn>
+  static int guarded(Fn &&fn) {
+    try {
+      return fn();
+    } catch (const std::bad_alloc &) {
+      return WAP_ENOMEM;
+    } catch (...) {
+      return WAP_EHOST;
+    }
+  }
+
+  // Stops and joins the workers (destruction, or a failed start).
+  void stop_workers() {
+    {
+      std::lock_guard<std::mutex> lk(m);
+      stop = true;
+    }
+    cv.notify_all();
+    for (auto &t : workers) t.join();
+    workers.clear();
+  }
+
   void worker() {
     cudaSetDevice(device);
     std::unique_lock<std::mutex> lk(m);
     while (!stop) {
       std::vector<Job *> admitted;
-      admit_locked(admitted);
+      try {
+        admit_locked(admitted);
+      } catch (const std::bad_alloc &) {  // no host memory for the list: admit nothing this round
+        admitted.clear();
+      }
       if (!admitted.empty()) {
         lk.unlock();
         for (Job *j : admitted) {
-          const int r = setup(j);
+          const int r = guarded([&] { return setup(j); });
           lk.lock();
           if (r != WAP_OK) {
             release_ctx(j);
@@ -169,7 +199,7 @@ struct wap_server {
         r = wap_outer_iteration_step(pick->ctx, &pick->desc.sched, (int)(k % pick->nsteps), nullptr);
         last = (k + 1 >= pick->total);
       }
-      if (r == WAP_OK && last) r = collect(pick);
+      if (r == WAP_OK && last) r = guarded([&] { return collect(pick); });
       if (last || r != WAP_OK) release_ctx(pick);
       lk.lock();
       if (r == WAP_OK) pick->info.steps = k + (k < pick->total ? 1 : 0);
@@ -192,19 +222,19 @@ int wap_server_create(wap_server **out, int device, size_t hbm_budget_bytes, int
   s->device = device;
   s->budget = hbm_budget_bytes;
   s->t0 = std::chrono::steady_clock::now();
-  for (int w = 0; w < workers; ++w) s->workers.emplace_back([p = s.get()] { p->worker(); });
+  try {
+    for (int w = 0; w < workers; ++w) s->workers.emplace_back([p = s.get()] { p->worker(); });
+  } catch (...) {
+    s->stop_workers();  // the ones that did start, before the server goes away
+    throw;
+  }
   *out = s.release();
   return WAP_OK;
 } WAP_CATCH
 
 void wap_server_destroy(wap_server *s) {
   if (!s) return;
-  {
-    std::lock_guard<std::mutex> lk(s->m);
-    s->stop = true;
-  }
-  s->cv.notify_all();
-  for (auto &t : s->workers) t.join();
+  s->stop_workers();
   for (auto &kv : s->jobs) s->release_ctx(kv.second.get());
   wap_trim_cache(s->device);  // the jobs' recycled device blocks
   delete s;
@@ -227,13 +257,24 @@ int wap_server_submit(wap_server *s, const wap_job_desc *job, long long *h_id) t
     j->info.device_bytes += wap::flow_pairs_bytes(sc.vol, job->sched.flow_scales, job->sched.flow_eta);
   if (j->info.device_bytes > s->budget) return WAP_ETOOBIG;
   std::lock_guard<std::mutex> lk(s->m);
+  // room for every job in the active list, so that a worker's push never
+  // allocates (a failure here leaves the server unchanged)
+  s->active.reserve(s->jobs.size() + 1);
   j->id = s->next_id++;
   j->info.state = WAP_JOB_QUEUED;
   j->info.status = WAP_OK;
   j->info.t_submit = s->now();
-  *h_id = j->id;
-  s->queue.push_back(j.get());
-  s->jobs.emplace(j->id, std::move(j));
+  Job *jp = j.get();
+  // the map takes ownership first; if the queue cannot take the job too, the
+  // map lets it go again, so a failed submit leaves no trace
+  auto ins = s->jobs.emplace(jp->id, std::move(j));
+  try {
+    s->queue.push_back(jp);
+  } catch (...) {
+    s->jobs.erase(ins.first);
+    throw;
+  }
+  *h_id = jp->id;
   s->cv.notify_all();
   return WAP_OK;
 } WAP_CATCH
