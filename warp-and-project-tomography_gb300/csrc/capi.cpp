@@ -91,6 +91,29 @@ size_t cache_trim(int dev) {  // dev < 0: every device
   return freed;
 }
 
+// CUDA events owned by one call, destroyed on every return path.
+struct ScopedEvents {
+  std::vector<cudaEvent_t> e;
+  explicit ScopedEvents(size_t n) : e(n, nullptr) {}
+  ScopedEvents(const ScopedEvents &) = delete;
+  ScopedEvents &operator=(const ScopedEvents &) = delete;
+  ~ScopedEvents() {
+    for (cudaEvent_t x : e)
+      if (x) cudaEventDestroy(x);
+  }
+  cudaError_t create() {
+    for (auto &x : e) {
+      const cudaError_t r = cudaEventCreate(&x);
+      if (r != cudaSuccess) {
+        x = nullptr;
+        return r;
+      }
+    }
+    return cudaSuccess;
+  }
+  cudaEvent_t operator[](size_t i) const { return e[i]; }
+};
+
 struct DevMem {
   void *p = nullptr;
   size_t bytes = 0;  // capacity
@@ -781,9 +804,9 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
       for (int z : zts)
         if (z >= 2 && z <= n[2] && (cand.back().first != 3 || cand.back().second != z)) cand.emplace_back(3, z);
   }
-  cudaEvent_t e0, e1;
-  CU(cudaEventCreate(&e0));
-  CU(cudaEventCreate(&e1));
+  ScopedEvents ev(2);
+  CU(ev.create());
+  const cudaEvent_t e0 = ev[0], e1 = ev[1];
   float best = 1e30f;
   std::pair<int, int> pick = cand.front();
   for (const auto &c : cand) {
@@ -799,8 +822,6 @@ int pd_plan(wap_ctx *ctx, const FlowDims &D, Launch &launch, int &form, int &zch
       pick = c;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   plans[key] = pick;
   {
     std::lock_guard<std::mutex> lk(g_plan_mutex);
@@ -1076,8 +1097,8 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
     }
   }
   const float aabb[6] = {0, (float)dims[0], 0, (float)dims[1], 0, (float)dims[2]};
-  std::vector<cudaEvent_t> lev(scales + 1);
-  for (auto &e : lev) CU(cudaEventCreate(&e));
+  ScopedEvents lev(scales + 1);
+  CU(lev.create());
   CU(cudaEventRecord(lev[0], ctx->stream));
   for (int l = 0; l < scales; ++l) {
     PyramidLevel &P = *ctx->pyramid[l];
@@ -1107,7 +1128,6 @@ int flow_multiscale(wap_ctx *ctx, const int dims[3], const float *I1, const floa
     CU(cudaEventElapsedTime(&ms, lev[l], lev[l + 1]));
     if (scales - 1 - l < 8) ctx->stats.ms_flow_level[scales - 1 - l] += ms;
   }
-  for (auto &e : lev) cudaEventDestroy(e);
   return WAP_OK;
 }
 
@@ -1321,7 +1341,8 @@ void wap_destroy(wap_ctx *ctx) {
   cudaSetDevice(ctx->device);
   const bool idle = !ctx->stream || cudaStreamSynchronize(ctx->stream) == cudaSuccess;
   cudaStream_t s = ctx->own_stream ? ctx->stream : nullptr;
-  for (cudaEvent_t e : ctx->pd_events) cudaEventDestroy(e);
+  for (cudaEvent_t e : ctx->pd_events)
+    if (e) cudaEventDestroy(e);
   g_recycle = idle;  // the stream has drained: the blocks go to the cache
   delete ctx;
   g_recycle = false;
@@ -1362,11 +1383,19 @@ int wap_get_stats(wap_ctx *ctx, wap_stats *out) try {
 
 int wap_set_profiling(wap_ctx *ctx, int on) try {
   CHECK(ctx, WAP_EINVAL, "null context");
-  ctx->profiling = on ? 1 : 0;
-  if (ctx->profiling && ctx->pd_events.empty()) {
-    ctx->pd_events.resize(2 * 50);
-    for (auto &e : ctx->pd_events) CU(cudaEventCreate(&e));
+  if (on && ctx->pd_events.empty()) {
+    std::vector<cudaEvent_t> ev(2 * 50, nullptr);
+    for (auto &e : ev) {
+      const cudaError_t r = cudaEventCreate(&e);
+      if (r != cudaSuccess) {  // none kept: profiling stays off
+        for (cudaEvent_t x : ev)
+          if (x) cudaEventDestroy(x);
+        return fail(ctx, WAP_ECUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(r));
+      }
+    }
+    ctx->pd_events.swap(ev);
   }
+  ctx->profiling = on ? 1 : 0;
   return WAP_OK;
 } WAP_CATCH
 
@@ -1747,8 +1776,8 @@ int wap_adaptive_warp(wap_ctx *ctx, int frame, int nb_warp, int cut, int exact) 
 int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1, wap_stats *stats) try {
   TRY(check_schedule(ctx, sch, f0, f1));
   ctx->stats = wap_stats{};
-  cudaEvent_t ev[4];
-  for (auto &e : ev) CU(cudaEventCreate(&e));
+  ScopedEvents ev(4);
+  CU(ev.create());
   CU(cudaEventRecord(ev[0], ctx->stream));
   // (1) CP prior + SART proximal steps (WaP_Tomo.cpp:563-698)
   for (int icp = 1; icp <= sch->n_cp; ++icp) TRY(cp_pass(ctx, sch, f0, f1, icp));
@@ -1762,7 +1791,6 @@ int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, in
   CU(cudaEventSynchronize(ev[3]));
   float ms[3];
   for (int q = 0; q < 3; ++q) CU(cudaEventElapsedTime(&ms[q], ev[q], ev[q + 1]));
-  for (auto &e : ev) cudaEventDestroy(e);
   ctx->stats.ms_cp = ms[0];
   ctx->stats.ms_flow = ms[1];
   ctx->stats.ms_wap = ms[2];
@@ -1780,9 +1808,9 @@ int wap_outer_iteration_step(wap_ctx *ctx, const wap_schedule *sch, int step, wa
   const int nflow = std::max(ctx->F - 1, 0);
   CHECK(step >= 0 && step < sch->n_cp + nflow + 1, WAP_EINVAL, "step out of range");
   ctx->stats = wap_stats{};
-  cudaEvent_t e0, e1;
-  CU(cudaEventCreate(&e0));
-  CU(cudaEventCreate(&e1));
+  ScopedEvents ev(2);
+  CU(ev.create());
+  const cudaEvent_t e0 = ev[0], e1 = ev[1];
   CU(cudaEventRecord(e0, ctx->stream));
   int phase = 0;
   if (step < sch->n_cp) {
@@ -1798,8 +1826,6 @@ int wap_outer_iteration_step(wap_ctx *ctx, const wap_schedule *sch, int step, wa
   CU(cudaEventSynchronize(e1));
   float ms = 0.0f;
   CU(cudaEventElapsedTime(&ms, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   (phase == 0 ? ctx->stats.ms_cp : phase == 1 ? ctx->stats.ms_flow : ctx->stats.ms_wap) = ms;
   if (stats) *stats = ctx->stats;
   return WAP_OK;
@@ -2025,9 +2051,9 @@ int batch_autotune(wap_batch *b, const wap_schedule *sch) {
   BatchPlan P;
   int best_step = 0, pick_fp = 0, pick_bp = 0;
   float best_fp = 1e30f, best_bp = 1e30f;
-  cudaEvent_t e0, e1;
-  BCU(cudaEventCreate(&e0));
-  BCU(cudaEventCreate(&e1));
+  ScopedEvents ev(2);
+  BCU(ev.create());
+  const cudaEvent_t e0 = ev[0], e1 = ev[1];
   int rc = WAP_OK;
   for (int shape = 0; shape < std::max(kFpShapes, kBpShapes) && rc == WAP_OK; ++shape) {
     b->fp_shape = std::min(shape, kFpShapes - 1);
@@ -2063,8 +2089,6 @@ int batch_autotune(wap_batch *b, const wap_schedule *sch) {
     if (shape < kFpShapes && ms[0] < best_fp) best_fp = ms[0], pick_fp = shape;
     if (shape < kBpShapes && ms[1] < best_bp) best_bp = ms[1], pick_bp = shape;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   b->fp_shape = keep_fp >= 0 ? keep_fp : pick_fp;
   b->bp_shape = keep_bp >= 0 ? keep_bp : pick_bp;
   return rc;
@@ -2188,9 +2212,9 @@ int wap_batch_outer_iteration(wap_batch *b, const wap_schedule *scheds, wap_stat
     x->stats = wap_stats{};
     BCU(stream_follow(b->stream, x->stream));  // the batch follows each scan's earlier work
   }
-  cudaEvent_t t0, t1;
-  BCU(cudaEventCreate(&t0));
-  BCU(cudaEventCreate(&t1));
+  ScopedEvents tev(2);
+  BCU(tev.create());
+  const cudaEvent_t t0 = tev[0], t1 = tev[1];
   BCU(cudaEventRecord(t0, b->stream));
   // (1) CP + SART: tune, plan, capture one CP iteration as a graph, replay it
   warm_queue_kernels();
@@ -2221,15 +2245,27 @@ int wap_batch_outer_iteration(wap_batch *b, const wap_schedule *scheds, wap_stat
   // (2) flows and (3) warp-and-project per scan, concurrently on their streams
   std::vector<int> rcs(n, WAP_OK);
   for (wap_ctx *x : b->ctxs) BCU(stream_follow(x->stream, b->stream));
-  std::vector<std::thread> th;
-  for (int c = 0; c < n; ++c)
-    th.emplace_back([&, c]() {
+  auto scan_rest = [&](int c) {  // one scan's flows and warp-and-project; exceptions become its status
+    try {
       wap_ctx *ctx = b->ctxs[c];
       int rc = cudaSetDevice(b->device) == cudaSuccess ? WAP_OK : WAP_ECUDA;
       for (int f = 0; rc == WAP_OK && f + 1 < ctx->F; ++f) rc = flow_pair(ctx, &scheds[c], f);
       if (rc == WAP_OK) rc = wap_pass(ctx, &scheds[c], 0, ctx->F);
       rcs[c] = rc;
-    });
+    } catch (const std::bad_alloc &) {
+      rcs[c] = WAP_ENOMEM;
+    } catch (...) {
+      rcs[c] = WAP_EHOST;
+    }
+  };
+  std::vector<std::thread> th;
+  int started = 0;
+  try {
+    th.reserve(n);
+    for (; started < n; ++started) th.emplace_back(scan_rest, started);
+  } catch (...) {  // no more threads: the remaining scans run here (same results, less overlap)
+  }
+  for (int c = started; c < n; ++c) scan_rest(c);
   for (auto &t : th) t.join();
   for (int c = 0; c < n; ++c)
     if (rcs[c] != WAP_OK) return bfail(b, rcs[c], "scan " + std::to_string(c) + ": " + b->ctxs[c]->err);
@@ -2238,8 +2274,6 @@ int wap_batch_outer_iteration(wap_batch *b, const wap_schedule *scheds, wap_stat
   BCU(cudaEventSynchronize(t1));
   float ms = 0.0f;
   BCU(cudaEventElapsedTime(&ms, t0, t1));
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
   if (stats) {
     wap_stats s{};
     for (wap_ctx *x : b->ctxs) {
