@@ -280,7 +280,7 @@ def cpu_sample(args, counts, threads):
     flow = P.rbf_flow(n, amp=3.0, seed=1)
     aabb = [0, n, 0, n, 0, n]
     t0 = time.time()
-    orc.advect([n] * 3, aabb, flow, vol, 0.5, 4)
+    warped = orc.advect([n] * 3, aabb, flow, vol, 0.5, 4)
     t["advect"] = time.time() - t0
     nv = n ** 3
     ytv = np.zeros((3, n, n, n), np.float32)
@@ -298,8 +298,11 @@ def cpu_sample(args, counts, threads):
     for lev in range(len(counts["pd_iterations_per_level"])):
         step = 1 << lev
         m = n // step
+        # a deforming pair (the volume and its warp by the smooth flow): with two
+        # near-identical images the CPU solver runs on subnormal duals, which
+        # the reference's flow pairs do not
         I1 = np.ascontiguousarray(vol[::step, ::step, ::step])
-        I2 = np.ascontiguousarray(v2[::step, ::step, ::step])
+        I2 = np.ascontiguousarray(warped.reshape(vol.shape)[::step, ::step, ::step])
         V = np.zeros((3, m, m, m), np.float32)
         Y = [np.zeros((3, m, m, m), np.float32) for _ in range(3)] + [np.zeros((m, m, m), np.float32)]
         orc.flow_level([m] * 3, I1, I2, V, *Y, 0.0, 0.05, pd_its - 1, 1, [0, m, 0, m, 0, m],
@@ -505,14 +508,30 @@ def run_gb300(args):
             t16 += e0.elapsed_time(e1) / 1e3
         ctx.set_tuning("flow_bits", 32)
         v16 = replicas.aggregate_rate(1, args.precision_steps / F, t16)
+        # Accuracy from identical state: one frame-step of a 3-frame scan of the
+        # same size in both arithmetics (precision_compare.py).
+        import precision_compare
+        acc = precision_compare.compare(torch, wap, n, d, args.nproj, args.flow_iters, args.scales)
         precision = {"flow_bits": 16, "value": v16, "unit": "outer-iter/s", "ms_per_step": t16 / args.precision_steps * 1e3,
                      "speedup_vs_fp32": v16 / value,
+                     "accuracy_from_identical_state": {
+                         "workload": "one frame-step of a 3-frame %d^3 foam-and-smoke scan (%d proj at %d^2), both "
+                                     "arithmetics from the same state (precision_compare.py)" % (n, args.nproj, d),
+                         "speedup": acc["precision_form"]["speedup"],
+                         "pd_iterations": {"reference_arithmetic": acc["reference_arithmetic"]["pd_iterations"],
+                                           "precision_form": acc["precision_form"]["pd_iterations"]},
+                         "volume_rel_l2_vs_reference_arithmetic":
+                             acc["precision_form"]["volume_rel_l2_vs_reference_arithmetic"],
+                         "flow_rel_l2_vs_reference_arithmetic":
+                             acc["precision_form"]["flow_rel_l2_vs_reference_arithmetic"]},
                      "note": "frame-steps of the frames after the timed ones, with the flow solver's dual, flow and "
                              "linearisation stored in FP16 (FP32 fused multiply-adds and hardware reciprocals in the "
-                             "primal-dual iteration), the projector reading FP16 brick copies with Kahan-compensated "
-                             "ray sums, and the FP32 backprojection in place of the reference's double bicubic; "
-                             "accuracy: tests/test_baseline_configs.py::test_256_precision_form_against_fp64_oracle "
-                             "(volume 1.5e-4, flow 1.1e-3 from the FP64 oracle at 256^3)"}
+                             "primal-dual iteration; its residual compares the stored states, so a level stops once "
+                             "the FP16 state no longer moves by the tolerance), the projector reading FP16 brick "
+                             "copies with Kahan-compensated ray sums, and the FP32 backprojection in place of the "
+                             "reference's double bicubic; at fixed iteration counts the volume is 1.5e-4 and the "
+                             "flow 1.1e-3 from the FP64 oracle at 256^3 "
+                             "(tests/test_baseline_configs.py::test_256_precision_form_against_fp64_oracle)"}
     e2e = replicas.aggregate_rate(world, K / F, t_e2e)
     pd_ms = agg["ms_pd"] / max(agg["pd_timed"], 1)
     achieved = PD_BYTES_MIN_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9

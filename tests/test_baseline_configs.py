@@ -316,7 +316,7 @@ def test_512_projection_bitexact_and_near_fp64(wapmod, orc, torch_cuda):
     over some 900 steps per ray, whose drift grows with the grid; 3.5e-6 at
     32^3): held to 1e-3."""
     import oracle as O
-    import precision_512 as P512
+    import precision_compare as P512
     torch = torch_cuda
     n, d, nproj = 512, 768, 360
     vol = P512.phantom(torch, n)

@@ -1,24 +1,27 @@
-"""The precision form at 512^3 x 768^2 (the precision configuration): one
-frame's share of an outer iteration, timed in the reference's arithmetic and
-in the precision form, with the precision form's distance from it.
+"""The precision form against the reference arithmetic on one frame's share
+of an outer iteration, from identical state: seconds in both arithmetics and
+the precision form's distance from the reference arithmetic.  The default is
+the precision configuration, 512^3 x 768^2; bench.py runs it at the
+benchmark's 256^3 x 384^2 for its precision line's accuracy.
 
-Workload (seeded, generated on the GPU): a 512^3 foam (band-limited noise
+Workload (seeded, generated on the GPU): an n^3 foam (band-limited noise
 thresholded at the 70th percentile: struts of density 1.0) overlaid with a
 smoke-like density from 3 octaves of value noise in [0, 0.6] (the larger of
 the two per voxel), moved by a divergence-free curl-noise velocity field of
-at most 8 voxels per frame; 360 cone-beam projections at 768x768 on
-golden-ratio angles; 3 frames (each frame's volume is the phantom advanced by
-its frame index), 1 % Gaussian noise on the projections of the run frame's
-window.  Schedule: PSART's 5 CP x 2 SART, a 4-level flow (tolerance 0.008,
-at most --flow-iters iterations, 3 warps), warp-and-project over the window.
+at most 8 voxels per frame; cone-beam projections on golden-ratio angles; 3
+frames (each frame's volume is the phantom advanced by its frame index), 1 %
+Gaussian noise on the projections of the run frame's window.  Schedule:
+PSART's 5 CP x 2 SART, a 4-level flow (tolerance 0.008, at most --flow-iters
+iterations, 3 warps), warp-and-project over the window.
 
 Reports JSON: seconds per frame-step in both arithmetics (each after an
 untimed short run that tunes the primal-dual plans of every pyramid level),
-and the precision form's relative L2 distance from the reference arithmetic
-for the frame's volume and flow.  The projector at this size is compared
-with the FP64 oracle in tests/test_baseline_configs.py.
+their primal-dual iteration counts, and the precision form's relative L2
+distance from the reference arithmetic for the frame's volume and flow.  The
+projector at 512^3 is compared with the FP64 oracle in
+tests/test_baseline_configs.py.
 
-    python precision_512.py [--n 512] [--det 768] [--flow-iters 3000]
+    python precision_compare.py [--n 512] [--det 768] [--nproj 360] [--flow-iters 3000]
 """
 import argparse
 import json
@@ -74,25 +77,13 @@ def curl_velocity(torch, n, vmax=8.0, seed=1):
     return (v * (vmax / v.abs().max())).contiguous()
 
 
-def main():
-    import torch
-
-    import build
-    import wap
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--n", type=int, default=512)
-    ap.add_argument("--det", type=int, default=768)
-    ap.add_argument("--nproj", type=int, default=360)
-    ap.add_argument("--flow-iters", type=int, default=3000)
-    ap.add_argument("--scales", type=int, default=4)
-    a = ap.parse_args()
-    build.build()
-    n, d, P = a.n, a.det, a.nproj
+def compare(torch, wap, n=512, d=768, P=360, flow_iters=3000, scales=4):
+    """One frame-step in the reference arithmetic and in the precision form,
+    from the same state; returns the report dict."""
     F, frame = 3, 1
     ang = (np.arange(P, dtype=np.float64) * 360.0 * 0.6180339887) % 360.0
     ctx = wap.Context(wap.make_scan((n, n, n), (d, d), P, nframes_cli=F), ang)
-    out = {"volume": n, "detector": d, "projections": P, "frames": F, "flow_iters": a.flow_iters,
-           "scales": a.scales}
+    out = {"volume": n, "detector": d, "projections": P, "frames": F, "flow_iters": flow_iters, "scales": scales}
     try:
         t0 = time.time()
         base = phantom(torch, n)
@@ -128,7 +119,7 @@ def main():
             for f in range(F):
                 ctx.upload_volume(f, host_vols[f])
             sched = wap.reference_schedule(n_cp=5, nb_sart=2, wp_frames=F, flow_iters=iters,
-                                           flow_scales=a.scales, flow_tol=0.008, cut=8, bp_exact=exact)
+                                           flow_scales=scales, flow_tol=0.008, cut=8, bp_exact=exact)
             ctx.synchronize()
             w0 = time.time()
             s = ctx.outer_iteration_frames(sched, frame, frame + 1)
@@ -140,8 +131,8 @@ def main():
 
         frame_step(32, 1, 2)  # untimed: tunes each level's primal-dual plan in both arithmetics
         frame_step(16, 0, 2)
-        sec32, s32, r32 = frame_step(32, 1, a.flow_iters)
-        sec16, s16, r16 = frame_step(16, 0, a.flow_iters)
+        sec32, s32, r32 = frame_step(32, 1, flow_iters)
+        sec16, s16, r16 = frame_step(16, 0, flow_iters)
 
         def rel(x, y):
             x, y = x.astype(np.float64), y.astype(np.float64)
@@ -156,7 +147,23 @@ def main():
                                  "flow_rel_l2_vs_reference_arithmetic": rel(r16[1], r32[1])}
     finally:
         ctx.close()
-    print(json.dumps(out))
+    return out
+
+
+def main():
+    import torch
+
+    import build
+    import wap
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--det", type=int, default=768)
+    ap.add_argument("--nproj", type=int, default=360)
+    ap.add_argument("--flow-iters", type=int, default=3000)
+    ap.add_argument("--scales", type=int, default=4)
+    a = ap.parse_args()
+    build.build()
+    print(json.dumps(compare(torch, wap, a.n, a.det, a.nproj, a.flow_iters, a.scales)))
 
 
 if __name__ == "__main__":
