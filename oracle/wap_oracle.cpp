@@ -366,9 +366,18 @@ inline void produce_ray(const ProjGeom &g, const int dims[3], real px, real py, 
   tfar = mac_min(mac_min(tmx[0], tmx[1]), tmx[2]);
 }
 
-void set_threads(int t) {
-  if (t > 0) omp_set_num_threads(t);
-}
+// OpenMP threads for one call (t > 0; 0 keeps the current count), restored
+// on return so that a call with its own count (advect's 4, as the reference's
+// advect hard-codes) does not change the calls after it.
+struct ThreadScope {
+  int prev;
+  explicit ThreadScope(int t) : prev(omp_get_max_threads()) {
+    if (t > 0) omp_set_num_threads(t);
+  }
+  ~ThreadScope() { omp_set_num_threads(prev); }
+  ThreadScope(const ThreadScope &) = delete;
+  ThreadScope &operator=(const ThreadScope &) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // Bicubic backprojection helpers (WaP_Tomo.cpp:208-222, double arithmetic)
@@ -484,7 +493,7 @@ void orc_geometry(const orc_scan *s, double angle_deg, real p2m[16], real m2v[16
 
 // GenerateImage_MT (TypicalRayProducer.core.h:123-225).
 void orc_forward(const orc_scan *s, double angle_deg, const real *vol, real *img, real *len, real *weight) {
-  set_threads(s->threads);
+  ThreadScope threads_scope(s->threads);
   ProjGeom g = make_geometry(s, angle_deg);
   const int W = s->det[0], H = s->det[1];
   const real sd = orc_sample_distance(s->vs);
@@ -540,7 +549,7 @@ void orc_correction(int n, const real *p, const real *ax, const real *len, real 
 }
 
 void orc_bp_voxel(const orc_scan *s, double angle_deg, const real *corr, const int box[6], int mode, real *vol) {
-  set_threads(s->threads);
+  ThreadScope threads_scope(s->threads);
   ProjGeom g = make_geometry(s, angle_deg);
   const int W = s->det[0], H = s->det[1];
   const int *d = s->vol;
@@ -582,7 +591,7 @@ void orc_bp_voxel(const orc_scan *s, double angle_deg, const real *corr, const i
 
 void orc_advect(const int dims[3], const real aabb[6], const real *vel, const real *src, int nc, real dt,
                 real *out, int threads) {
-  set_threads(threads);
+  ThreadScope threads_scope(threads);
   const size_t nv = (size_t)dims[0] * dims[1] * dims[2];
   const real tdt = -dt;  // advect calls trace(..., -dt)
 #pragma omp parallel for schedule(dynamic, 1)
