@@ -298,9 +298,8 @@ def cpu_sample(args, counts, threads):
     for lev in range(len(counts["pd_iterations_per_level"])):
         step = 1 << lev
         m = n // step
-        # a deforming pair (the volume and its warp by the smooth flow): with two
-        # near-identical images the CPU solver runs on subnormal duals, which
-        # the reference's flow pairs do not
+        # a deforming pair (the volume and its warp by the smooth flow), as the
+        # reference's frame pairs are
         I1 = np.ascontiguousarray(vol[::step, ::step, ::step])
         I2 = np.ascontiguousarray(warped.reshape(vol.shape)[::step, ::step, ::step])
         V = np.zeros((3, m, m, m), np.float32)
