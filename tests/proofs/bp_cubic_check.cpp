@@ -1,7 +1,9 @@
 // Host check of the certified float-float bicubic (csrc/bp_cubic.h) against
 // the reference's double expression (WaP_Tomo.cpp:208-222, 1618): whenever
 // cubic_cert / update_cert claim a result, it must equal the double
-// expression rounded to float, bit for bit.  Inputs: correction-image-like
+// expression rounded to float, bit for bit.  The same for grow_cert against
+// CImg's cubic growth in double (CImg.h:28432-28610) with random double
+// weights t, t*t, (t*t)*t.  Inputs: correction-image-like
 // values of many magnitudes, exact ties and cancellations, random bit
 // patterns, and the interpolation weights the backprojection produces
 // (multiples of 2^-22 in [0, 1)).  Prints counts; exits 1 on any mismatch.
@@ -20,6 +22,14 @@ static float cubic_double(float p0, float p1, float p2, float p3, float x) {
   // subtractions inside, everything else in double
   return (float)(p1 + 0.5 * x * ((float)(p2 - p0) + x * (2.0 * p0 - 5.0 * p1 + 4.0 * p2 - p3 +
                                                          x * (3.0 * (float)(p1 - p2) + p3 - p0))));
+}
+
+static float grow_double(float v0, float v1, float v2, float v3, double t, double t2, double t3) {
+  // the flow pyramid's growth, as CImg evaluates it in double
+  const double val0 = v0, val1 = v1, val2 = v2, val3 = v3;
+  const double val = val1 + 0.5f * (t * (-val0 + val2) + t2 * (2 * val0 - 5 * val1 + 4 * val2 - val3) +
+                                    t3 * (-val0 + 3 * val1 - 3 * val2 + val3));
+  return (float)val;
 }
 
 static uint64_t s_state;
@@ -60,7 +70,7 @@ static float sample(int mode, float base) {
 int main(int argc, char **argv) {
   const long long cases = argc > 1 ? atoll(argv[1]) : 20000000;
   s_state = argc > 2 ? strtoull(argv[2], 0, 10) : 12345;
-  long long claimed = 0, bad = 0, u_claimed = 0, u_bad = 0;
+  long long claimed = 0, bad = 0, u_claimed = 0, u_bad = 0, g_claimed = 0, g_bad = 0;
   const double alpha = 0.1;  // the reference's default -a
   const float ah = (float)alpha, al = (float)(alpha - (double)ah);
   for (long long c = 0; c < cases; ++c) {
@@ -80,6 +90,27 @@ int main(int argc, char **argv) {
         ++bad;
       }
     }
+    {
+      double t = unif();  // an accumulated offset's fraction, any double in [0, 1)
+      if ((rnd() & 15) == 0) t = 0.0;
+      if ((rnd() & 15) == 1) t = 0.5;
+      const double t2 = t * t, t3 = t2 * t;
+      float tp[6];
+      const double w[3] = {t, t2, t3};
+      for (int q = 0; q < 3; ++q) {
+        tp[2 * q] = (float)w[q];
+        tp[2 * q + 1] = (float)(w[q] - (double)tp[2 * q]);
+      }
+      if (wap::bpc::grow_cert(p0, p1, p2, p3, tp, &got)) {
+        ++g_claimed;
+        const float want = grow_double(p0, p1, p2, p3, t, t2, t3);
+        if (fbits(got) != fbits(want)) {
+          if (g_bad < 10)
+            printf("grow mismatch: v=(%a %a %a %a) t=%a got %a want %a\n", p0, p1, p2, p3, t, got, want);
+          ++g_bad;
+        }
+      }
+    }
     const float v = fabsf(sample(mode == 4 ? 0 : mode, base));
     const float g = sample(mode, base);
     if (wap::bpc::update_cert(v, g, ah, al, &got)) {
@@ -91,7 +122,8 @@ int main(int argc, char **argv) {
       }
     }
   }
-  printf("cases=%lld cubic-claimed=%lld cubic-mismatch=%lld update-claimed=%lld update-mismatch=%lld\n", cases,
-         claimed, bad, u_claimed, u_bad);
-  return (bad || u_bad) ? 1 : 0;
+  printf("cases=%lld cubic-claimed=%lld cubic-mismatch=%lld update-claimed=%lld update-mismatch=%lld "
+         "grow-claimed=%lld grow-mismatch=%lld\n",
+         cases, claimed, bad, u_claimed, u_bad, g_claimed, g_bad);
+  return (bad || u_bad || g_bad) ? 1 : 0;
 }

@@ -1,5 +1,6 @@
-"""The certified float-float evaluation of the reference's double bicubic
-(csrc/bp_cubic.h), checked on the host: whenever it claims a float result,
+"""The certified float-float evaluation of the reference's double bicubic and
+of the flow pyramid's double cubic growth (csrc/bp_cubic.h), checked on the
+host: whenever it claims a float result,
 that result equals the reference's double expression rounded to float, bit
 for bit, over tens of millions of correction-image-like, cancelling, tied and
 random-bit-pattern inputs.  The exact backprojection kernel takes the double
@@ -30,7 +31,9 @@ def checker(tmp_path_factory):
 def test_certified_bicubic_matches_double(checker, seed):
     r = subprocess.run([checker, "10000000", seed], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
-    out = dict(kv.split("=") for kv in r.stdout.split()[-5:])
+    out = dict(kv.split("=") for kv in r.stdout.split()[-7:])
     assert out["cubic-mismatch"] == "0" and out["update-mismatch"] == "0", r.stdout
-    # the certificate must also be useful: it decides nearly all cases
+    assert out["grow-mismatch"] == "0", r.stdout
+    # the certificates must also be useful: they decide nearly all cases
     assert int(out["cubic-claimed"]) > 0.95 * int(out["cases"]), r.stdout
+    assert int(out["grow-claimed"]) > 0.95 * int(out["cases"]), r.stdout

@@ -1,5 +1,7 @@
-// The reference's bicubic weights in double (WaP_Tomo.cpp:208-222), evaluated
-// without the FP64 pipe where the result is certain.
+// The reference's cubics in double, evaluated without the FP64 pipe where the
+// result is certain: the backprojection's bicubic weights (WaP_Tomo.cpp:
+// 208-222, cubic_cert below) and the flow pyramid's cubic growth (CImg.h:
+// 28432-28610, grow_cert at the end).
 //
 // cubicInterpolate(float p[4], float x) computes, in C's promotion order,
 //   p1 + (0.5 x) * ((p2 - p0)_f + x * ((((2 p0 - 5 p1) + 4 p2) - p3)
@@ -167,6 +169,45 @@ BPC_HD bool update_cert(float v, float g, float ah, float al, float *out) {
   const FF r = ff_add_f(p, v);
   const float t = fma_up(fabsf(ah), fabsf(g), fabsf(v));
   return certain_rounding(r, bound(t), out);
+}
+
+// a * (bh + bl) for a float-float a and a double weight given as the float
+// pair bh + bl: the leading product exactly (two_prod), the cross terms with
+// one rounding each, a.l * bl (below 2^-48 of the product) dropped.
+BPC_HD FF ff_mul_pair(FF a, float bh, float bl) {
+  const FF p = two_prod(a.h, bh);
+  return fast_two_sum(p.h, fma(a.h, bl, fma(a.l, bh, p.l)));
+}
+
+// CImg's cubic growth of an image axis (CImg.h:28432-28610, interpolation
+// type 5), which the flow pyramid evaluates in double:
+//   val1 + 0.5 (t (-val0 + val2) + t2 (((2 val0 - 5 val1) + 4 val2) - val3)
+//               + t3 (((-val0 + 3 val1) - 3 val2) + val3))
+// with float samples val0..val3 and the double weights t, t2 = t t and
+// t3 = t2 t, each passed as a float pair tp[2q] + tp[2q+1] within 2^-48 of
+// it; the caller stores the double result in a float.  Certified as
+// cubic_cert is: at most 21 float-float operations (counting the weights'
+// representation) put the float-float value within 2^-41.6 T of the exact
+// value and the double evaluation's 13 roundings within 2^-49.3 T, so the
+// same B = 2^-40 T + 2^-126 covers both.
+BPC_HD bool grow_cert(float v0, float v1, float v2, float v3, const float *tp, float *out) {
+  const FF A = two_sum(-v0, v2);
+  FF B = ff_add_f(ff_add_f(ff_add_f(two_prod(-5.0f, v1), mul(2.0f, v0)), mul(4.0f, v2)), -v3);
+  FF C = ff_add(ff_add_f(two_prod(3.0f, v1), -v0), two_prod(-3.0f, v2));
+  C = ff_add_f(C, v3);
+  FF S = ff_add(ff_mul_pair(A, tp[0], tp[1]), ff_mul_pair(B, tp[2], tp[3]));
+  S = ff_add(S, ff_mul_pair(C, tp[4], tp[5]));
+  const FF val = ff_add_f(FF{mul(0.5f, S.h), mul(0.5f, S.l)}, v1);
+  // T: the same tree on absolute values, rounded upward
+  const float a0 = fabsf(v0), a1 = fabsf(v1), a2 = fabsf(v2), a3 = fabsf(v3);
+  const float w1 = add_up(fabsf(tp[0]), fabsf(tp[1])), w2 = add_up(fabsf(tp[2]), fabsf(tp[3])),
+              w3 = add_up(fabsf(tp[4]), fabsf(tp[5]));
+  const float sa = add_up(a0, a2);
+  const float sb = add_up(add_up(fma_up(5.0f, a1, mul(2.0f, a0)), mul(4.0f, a2)), a3);
+  const float sc = add_up(fma_up(3.0f, a2, fma_up(3.0f, a1, a0)), a3);
+  const float ts = fma_up(w3, sc, fma_up(w2, sb, mul_up(w1, sa)));
+  const float t = fma_up(0.5f, ts, a1);
+  return certain_rounding(val, bound(t), out);
 }
 
 }  // namespace bpc

@@ -631,7 +631,7 @@ int resize_tables(wap_ctx *ctx, int Sin, int Sout, ResizeTables &tb) {
   auto it = ctx->resize_tables.find(key);
   if (it == ctx->resize_tables.end()) {
     HostResizeAxis h = make_resize_axis(Sin, Sout);
-    std::unique_ptr<DevMem[]> m(new DevMem[5]);
+    std::unique_ptr<DevMem[]> m(new DevMem[6]);
     TRY(upload(ctx, m[0], h.tap_start));
     TRY(upload(ctx, m[1], h.tap_src));
     TRY(upload(ctx, m[2], h.tap_w));
@@ -646,6 +646,14 @@ int resize_tables(wap_ctx *ctx, int Sin, int Sout, ResizeTables &tb) {
       f3[3 * o + 2] = t2 * t;
     }
     TRY(upload(ctx, m[4], f3));
+    // the same weights as float pairs hi + lo (|w - (hi + lo)| <= 2^-48 |w|)
+    // for the certified float-float growth
+    std::vector<float> ff(2 * f3.size());
+    for (size_t q = 0; q < f3.size(); ++q) {
+      ff[2 * q] = (float)f3[q];
+      ff[2 * q + 1] = (float)(f3[q] - (double)ff[2 * q]);
+    }
+    TRY(upload(ctx, m[5], ff));
     it = ctx->resize_tables.emplace(key, std::move(m)).first;
   }
   tb.tap_start = it->second[0].as<int>();
@@ -653,6 +661,7 @@ int resize_tables(wap_ctx *ctx, int Sin, int Sout, ResizeTables &tb) {
   tb.tap_w = it->second[2].as<float>();
   tb.base = it->second[3].as<int>();
   tb.frac = it->second[4].as<double>();
+  tb.frac_ff = it->second[5].as<float>();
   return WAP_OK;
 }
 

@@ -26,6 +26,7 @@ struct ResizeTables {
   const float *tap_w = nullptr;
   const int *base = nullptr;       // Sout
   const double *frac = nullptr;    // 3 * Sout: t, t*t, t*t*t per output cell
+  const float *frac_ff = nullptr;  // 6 * Sout: each of those as a float pair hi + lo
 };
 
 DericheCoefs deriche_coefs(float sigma);
