@@ -920,8 +920,11 @@ int orc_flow_level(const int dims[3], const real *I1, const real *I2, real *V, r
         p += pp;
       }
       // dual (optical_flow.h:567-813), norm != 4 branch
-      auto dual = [&](int t, real &acc) {
-        int i = t % dims[0], j = (t / dims[0]) % dims[1], k = t / (dims[0] * dims[1]);
+      // over every voxel in index order (the reference's flat tmpIndex loop with
+      // its i/j/k tables; nested loops here give the same order without a
+      // division per voxel)
+      auto dual = [&](int i, int j, int k, real &acc) {
+        const size_t t = g.id(i, j, k);
         if (res) {
           for (int q = 0; q < 9; ++q) yOld[q][t] = y[q][t];
           y4Old[t] = y4[t];
@@ -950,11 +953,15 @@ int orc_flow_level(const int dims[3], const real *I1, const real *I2, real *V, r
         }
       };
       if (deterministic) {
-        for (int t = 0; t < nPx; ++t) dual(t, d);
+        for (int k = 0; k < dims[2]; ++k)
+          for (int j = 0; j < dims[1]; ++j)
+            for (int i = 0; i < dims[0]; ++i) dual(i, j, k, d);
       } else {
         real dd = 0.0f;
 #pragma omp parallel for reduction(+ : dd)
-        for (int t = 0; t < nPx; ++t) dual(t, dd);
+        for (int k = 0; k < dims[2]; ++k)
+          for (int j = 0; j < dims[1]; ++j)
+            for (int i = 0; i < dims[0]; ++i) dual(i, j, k, dd);
         d += dd;
       }
       if (res) err = (d * d + p * p) / (real)nPx;
