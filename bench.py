@@ -10,10 +10,11 @@ schedule of PSART::Render: 5 CP iterations x 2 SART sweeps, a 4-level L1-TV
 flow (tol 0.008, lambda 0.05, <= 3000 iterations, 3 warps) for every
 adjacent pair, then warp-and-project over every frame's window.
 
-A "step" is one frame's complete share of an outer iteration (its CP + SART
-steps, the flow of the pair it starts, its warp-and-project window): an
-outer iteration is exactly F such steps, so value = outer-iter/s =
-1 / (F * mean step time).  A whole outer iteration at this size is minutes of
+A "step" is the complete share of an outer iteration of --frames-per-step
+consecutive frames (2 by default: their CP + SART steps, the flow pairs they
+start, which run concurrently on the library's flow lanes, their
+warp-and-project windows): an outer iteration is exactly F / 2 such steps, so
+value = outer-iter/s = 2 / (F * mean step time).  A whole outer iteration at this size is minutes of
 GPU time, which is why the unit streamed here is the frame share.
 
 value times the steps on the device with inputs resident; e2e times the same
@@ -91,6 +92,11 @@ def parse():
                     help="primal-dual iterations per level and warp of the batched scans' flows")
     ap.add_argument("--kernel-reps", type=int, default=5,
                     help="timed launches per kernel of the line's per-kernel roofline table (0: skip)")
+    ap.add_argument("--frames-per-step", type=int, default=2,
+                    help="consecutive frames a step covers: their CP and SART work, their flow pairs (which run "
+                         "concurrently on the library's flow lanes) and their warp-and-project windows")
+    ap.add_argument("--flow-lanes", type=int, default=2,
+                    help="flow pairs the library runs concurrently (its flow_lanes tuning key)")
     ap.add_argument("--full-outer", action="store_true",
                     help="also time one whole outer iteration (all frames in pass order; minutes at 256^3)")
     ap.add_argument("--save-outer-counts", default="",
@@ -124,12 +130,15 @@ def outer_counts(args):
 
 def bench_config(args, F):
     """The workload's config object, shared by both arms."""
+    fs = getattr(args, "frames_per_step", 2)
     return {"workload": "256^3 volume, 192 proj at 384^2, 48 frames, 5 CP x 2 SART, 4-level L1-TV flow "
-                        "(tol 0.008, <=3000 its, 3 warps), WaP over all windows; step = one frame's share "
-                        "of an outer iteration" if (args.n, args.det, args.nproj) == (256, 384, 192) else
+                        "(tol 0.008, <=3000 its, 3 warps), WaP over all windows" if (args.n, args.det, args.nproj) ==
+                        (256, 384, 192) else
                         "%d^3 volume, %d proj at %d^2, %d frames, 5 CP x 2 SART, %d-level L1-TV flow (tol 0.008, "
-                        "<=%d its, 3 warps), WaP over all windows; step = one frame's share of an outer iteration"
+                        "<=%d its, 3 warps), WaP over all windows"
                         % (args.n, args.nproj, args.det, F, args.scales, args.flow_iters),
+            "step": "%d consecutive frames' share of an outer iteration (their CP and SART work, their flow pairs, "
+                    "their warp-and-project windows); %d steps make one outer iteration" % (fs, F // fs),
             "volume": [args.n] * 3, "detector": [args.det] * 2, "projections": args.nproj, "frames": F,
             "parallelism": "single", "l2": "working set > L2 (GBs per step)",
             "bp_arithmetic": "reference double (exact)"}
@@ -384,6 +393,28 @@ def kernel_table(ctx, torch, stream, args, frame, peak):
     ms = timed(lambda: ctx.sart_prox(frame, nb_sart=1, cut=cut, exact=1)) / win
     row("sart_step (exact BP; one SART sweep over the %d-projection window / %d)" % (win, win), ms,
         3 * nv * 4 + 20 * D)
+    # One flow primal-dual iteration at this size with the GPU to itself: a
+    # compute context on the bench's stream runs 60 iterations of a flow level
+    # on the frame's volume pair, every tenth launch timed (in the timed region
+    # the flow lanes run two pairs at once, so there a launch shares the GPU).
+    pc = wap.Context(None, None)
+    try:
+        pc.set_stream(stream.cuda_stream)
+        pc.set_profiling(True)
+        with torch.cuda.stream(stream):
+            I2 = torch.from_numpy(ctx.download_volume(frame + 1)).cuda()
+            V = torch.zeros((3, n, n, n), device="cuda")
+            Y = [torch.zeros((3, n, n, n), device="cuda") for _ in range(3)] + [torch.zeros((n, n, n), device="cuda")]
+        stream.synchronize()
+        pc.flow_level([n] * 3, vol, I2, V, *Y, 0.0, 0.05, 59, 1, [0, n, 0, n, 0, n], [8] * 6)
+        pc.synchronize()
+        st_pd = pc.stats()
+        ms = st_pd.ms_pd / max(st_pd.pd_timed, 1)
+        row("pd_iteration (one flow primal-dual iteration, the GPU to itself)", ms, PD_BYTES_MIN_PER_VOXEL * nv,
+            launches_timed=int(st_pd.pd_timed))
+        del V, Y, I2
+    finally:
+        pc.close()
     ctx.upload_volume(frame, saved_vol)
     return rows
 
@@ -408,6 +439,7 @@ def run_gb300(args):
     F = meta["nframes"]
     ctx.set_projections_device(projs)
     ctx.set_tuning("flow_bits", args.flow_bits)
+    ctx.set_tuning("flow_lanes", args.flow_lanes)
     ctx.level_setup(0)
     sched = wap.reference_schedule(n_cp=5, nb_sart=2, wp_frames=F, flow_iters=args.flow_iters,
                                    flow_scales=args.scales, flow_tol=0.008, cut=8, bp_exact=1)
@@ -432,13 +464,16 @@ def run_gb300(args):
         ctx.call("wap_frame_volume_download", f, h_vol.data_ptr())
         ctx.call("wap_frame_flow_download", f, h_flow.data_ptr())
 
-    order = replicas.frame_order(rank, args.warmup + args.steps, F)
+    FS = args.frames_per_step
+    order = replicas.frame_order(rank, args.warmup + args.steps, F, span=FS)
     for i in range(args.warmup):
         f = order[i]
         with torch.cuda.stream(stream):
-            projs[int(st[f]):int(en[f]) + 1].copy_(h_projs[int(st[f]):int(en[f]) + 1], non_blocking=True)
-        ctx.outer_iteration_frames(sched, f, f + 1)
-        d2h(f)
+            projs[int(st[f]):int(en[f + FS - 1]) + 1].copy_(h_projs[int(st[f]):int(en[f + FS - 1]) + 1],
+                                                           non_blocking=True)
+        ctx.outer_iteration_frames(sched, f, f + FS)
+        for g in range(f, f + FS):
+            d2h(g)
     stream.synchronize()
     if dist:
         dist.barrier()
@@ -455,15 +490,16 @@ def run_gb300(args):
     for i in range(args.warmup, args.warmup + args.steps):
         f = order[i]
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        s0, s1 = int(st[f]), int(en[f]) + 1
+        s0, s1 = int(st[f]), int(en[f + FS - 1]) + 1
         with torch.cuda.stream(stream):
             ev[0].record(stream)
             projs[s0:s1].copy_(h_projs[s0:s1], non_blocking=True)
             ev[1].record(stream)
-        s = ctx.outer_iteration_frames(sched, f, f + 1)
+        s = ctx.outer_iteration_frames(sched, f, f + FS)
         with torch.cuda.stream(stream):
             ev[2].record(stream)
-            d2h(f)
+            for g in range(f, f + FS):
+                d2h(g)
             ev[3].record(stream)
         stream.synchronize()
         t_dev += ev[1].elapsed_time(ev[2]) / 1e3
@@ -482,7 +518,7 @@ def run_gb300(args):
         t_dev, t_e2e = replicas.max_over_ranks([t_dev, t_e2e], tdist, device="cuda")
         tdist.barrier()
     K = args.steps
-    value = replicas.aggregate_rate(world, K / F, t_dev)
+    value = replicas.aggregate_rate(world, K * FS / F, t_dev)
     pd_side = round(pd_vox ** (1.0 / 3.0))
     form, zchunk = ctx.get_tuning([pd_side] * 3)
     level_plans = [list(ctx.get_tuning([int(n * 0.5 ** l)] * 3)) for l in range(args.scales)]
@@ -494,19 +530,19 @@ def run_gb300(args):
         sched16 = wap.reference_schedule(n_cp=5, nb_sart=2, wp_frames=F, flow_iters=args.flow_iters,
                                          flow_scales=args.scales, flow_tol=0.008, cut=8, bp_exact=0)
         t16 = 0.0
-        porder = replicas.frame_order(rank, args.warmup + args.steps + args.precision_steps, F)
+        porder = replicas.frame_order(rank, args.warmup + args.steps + args.precision_steps, F, span=FS)
         for i in range(args.warmup, args.warmup + args.precision_steps):
             f = porder[args.steps + i]  # frames after the timed ones
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             with torch.cuda.stream(stream):
                 e0.record(stream)
-            ctx.outer_iteration_frames(sched16, f, f + 1)
+            ctx.outer_iteration_frames(sched16, f, f + FS)
             with torch.cuda.stream(stream):
                 e1.record(stream)
             stream.synchronize()
             t16 += e0.elapsed_time(e1) / 1e3
         ctx.set_tuning("flow_bits", 32)
-        v16 = replicas.aggregate_rate(1, args.precision_steps / F, t16)
+        v16 = replicas.aggregate_rate(1, args.precision_steps * FS / F, t16)
         # Accuracy from identical state: one frame-step of a 3-frame scan of the
         # same size in both arithmetics (precision_compare.py).
         import precision_compare
@@ -531,7 +567,7 @@ def run_gb300(args):
                              "reference's double bicubic; at fixed iteration counts the volume is 1.5e-4 and the "
                              "flow 1.1e-3 from the FP64 oracle at 256^3 "
                              "(tests/test_baseline_configs.py::test_256_precision_form_against_fp64_oracle)"}
-    e2e = replicas.aggregate_rate(world, K / F, t_e2e)
+    e2e = replicas.aggregate_rate(world, K * FS / F, t_e2e)
     pd_ms = agg["ms_pd"] / max(agg["pd_timed"], 1)
     achieved = PD_BYTES_MIN_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9
     contract = PD_BYTES_PER_VOXEL * pd_vox / (pd_ms / 1e3) / 1e9
@@ -539,6 +575,7 @@ def run_gb300(args):
     kernels = None
     if rank == 0 and args.kernel_reps > 0:
         kernels = kernel_table(ctx, torch, stream, args, order[args.warmup], peak)
+    pd_alone = next((r for r in (kernels or []) if r["kernel"].startswith("pd_iteration")), None)
     full = None
     if args.full_outer:
         # One whole outer iteration, all frames in pass order (CP passes over all
@@ -572,7 +609,7 @@ def run_gb300(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded foam phantom, RBF+compression, Poisson I0=1e4)",
         "config": dict(bench_config(args, F), parallelism="replicas" if world > 1 else "single"),
         "e2e": {"value": e2e, "unit": "outer-iter/s", "h2d_bytes_per_step": h2d_bytes // K,
-                "d2h_bytes_per_step": 4 * nv * 4},
+                "d2h_bytes_per_step": FS * 4 * nv * 4},
         "gpu_launches": int(agg["kernel_launches"]),
         "roofline": {"kernel": "one flow primal-dual iteration at %d^3: %s (z-chunk %d, autotuned)"
                                % (pd_side, PD_FORMS.get(form, "?"), zchunk), "bound": "hbm",
@@ -587,14 +624,21 @@ def run_gb300(args):
                      "note": "achieved counts the 120 B/voxel a single-pass iteration must move (read and write the "
                              "dual y (10 words) and the flow v (3) once, read the linearisation u (4)); the "
                              "two-kernel contract figure, 208 B/voxel, is kept as contract_*",
-                     "ms_per_launch": pd_ms, "launches_timed": int(agg["pd_timed"])},
+                     "ms_per_launch": pd_ms, "launches_timed": int(agg["pd_timed"]),
+                     "alone": ({"ms_per_launch": pd_alone["ms_per_launch"], "achieved": pd_alone["achieved_gbs"],
+                                "frac": pd_alone["frac"],
+                                "note": "the same kernel with the GPU to itself (60 iterations of a flow level on the "
+                                        "run's frame pair, every tenth launch timed); in the timed region the flow "
+                                        "lanes run two pairs at once, so a launch there shares the GPU with the other "
+                                        "pair's work and takes longer while the step as a whole finishes sooner"}
+                               if pd_alone else None)},
         "phase_ms_per_step": {"cp_sart": agg["ms_cp"] / K, "flow": agg["ms_flow"] / K, "wap": agg["ms_wap"] / K},
         "pd_iterations_per_step": agg["flow_pd_iterations"] / K,
         "flow_levels_finest_first": {"sides": [int(n * 0.5 ** l) for l in range(args.scales)],
                                      "ms_per_step": [v / K for v in lev_ms],
                                      "pd_iterations_per_step": [v / K for v in lev_its],
                                      "pd_form_and_zchunk": level_plans},
-        "op_counts_per_outer_iteration": {k: agg[k] * F / K for k in ("projections", "backprojections",
+        "op_counts_per_outer_iteration": {k: agg[k] * F / (K * FS) for k in ("projections", "backprojections",
                                                                        "advect_voxels", "cp_frame_passes",
                                                                        "pd_voxel_iters")},
         "clocks": clk,
@@ -611,8 +655,8 @@ def run_gb300(args):
         counts = outer_counts(args)
         source = "measured counts of one whole outer iteration (%s)" % os.path.relpath(OUTER_COUNTS, REPO)
         if counts is None:
-            counts = {k: agg[k] * F / K for k in COUNT_KEYS}
-            counts["pd_iterations_per_level"] = [x * F / K for x in lev_its]
+            counts = {k: agg[k] * F / (K * FS) for k in COUNT_KEYS}
+            counts["pd_iterations_per_level"] = [x * F / (K * FS) for x in lev_its]
             source = "counts of the timed frame-steps, times frames / steps"
         threads = os.cpu_count() or 1
         w0 = time.time()

@@ -10,6 +10,7 @@
 // 256^3 frame does.  Nothing here falls back to the CPU: every numeric step
 // is a kernel in this library, and a missing GPU is an error.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdint>
@@ -17,7 +18,9 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
+#include <thread>
 #include <tuple>
 #include <vector>
 
@@ -245,6 +248,9 @@ struct wap_ctx {
   int pd_form = 0;    // 0: autotuned, 1: fused kernel, 2: primal + dual kernels
   int pd_zchunk = 0;  // 0: autotuned / default
   int flow_bits = 32; // 16: the flow solver's y, v, u stored in FP16 (the precision form)
+  int flow_lanes = 2; // flow pairs of an outer iteration run concurrently on this many lanes (1: in turn)
+  std::vector<wap_ctx *> lanes;  // the lanes: helper compute contexts, each with its own stream and workspaces
+  std::set<std::tuple<int, int, int, int, int, int>> lanes_tuned;  // flow shapes whose plans are tuned
   std::map<std::tuple<int, int, int>, std::pair<int, int>> pd_plans;  // grid -> (form, zchunk)
   std::map<std::tuple<int, int, int>, std::pair<int, int>> pd_plans16;  // the same for FP16 storage
   wap_observer_fn observer = nullptr;
@@ -1195,6 +1201,125 @@ int flow_pair(wap_ctx *ctx, const wap_schedule *sch, int f) {
   return WAP_OK;
 }
 
+void merge_flow_stats(wap_stats &d, const wap_stats &s) {
+  d.flow_pd_iterations += s.flow_pd_iterations;
+  d.kernel_launches += s.kernel_launches;
+  d.pd_voxel_iters += s.pd_voxel_iters;
+  d.advect_voxels += s.advect_voxels;
+  for (int l = 0; l < 8; ++l) {
+    d.ms_flow_level[l] += s.ms_flow_level[l];
+    d.pd_iters_level[l] += s.pd_iters_level[l];
+  }
+  if (s.pd_timed_voxels > d.pd_timed_voxels) {
+    d.pd_timed_voxels = s.pd_timed_voxels;
+    d.ms_pd = s.ms_pd;
+    d.pd_timed = s.pd_timed;
+  } else if (s.pd_timed_voxels == d.pd_timed_voxels) {
+    d.ms_pd += s.ms_pd;
+    d.pd_timed += s.pd_timed;
+  }
+}
+
+// The flow pairs of frames [f0, f1) (WaP_Tomo.cpp:732-777).  A pair reads two
+// frames' volumes and writes its own flow, so the pairs are independent: with
+// flow_lanes > 1 they run concurrently, each lane a helper compute context
+// with its own stream and flow workspaces, fed by its own host thread and
+// taking the next pair from a shared counter.  While one pair's finest level
+// streams from HBM, another's coarse levels and 128^3 level, latency-bound
+// on their own, fill the gaps.  Each pair's flow is the one it gets alone.
+// The pairs run in turn when an observer is set (its events come in pair
+// order), when one pair is due, and the first time a flow shape is seen, so
+// that the autotuner times its candidates undisturbed.
+int flow_phase(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
+  std::vector<int> pairs;
+  for (int f = f0; f < f1 && f + 1 < ctx->F; ++f) pairs.push_back(f);
+  const auto shape = std::make_tuple(ctx->scan.vol[0], ctx->scan.vol[1], ctx->scan.vol[2], sch->flow_scales,
+                                     ctx->flow_bits, (int)std::lround(sch->flow_eta * 1e6));
+  size_t first = 0;
+  if (!ctx->lanes_tuned.count(shape) && !pairs.empty()) {
+    TRY(flow_pair(ctx, sch, pairs[0]));
+    ctx->lanes_tuned.insert(shape);
+    first = 1;
+  }
+  const int K = std::min<int>(ctx->flow_lanes, (int)(pairs.size() - first));
+  if (K <= 1 || ctx->observer) {
+    for (size_t i = first; i < pairs.size(); ++i) TRY(flow_pair(ctx, sch, pairs[i]));
+    return WAP_OK;
+  }
+  while ((int)ctx->lanes.size() < K) {
+    wap_ctx *h = nullptr;
+    const int r = wap_create_compute(&h, ctx->device);
+    CHECK(r == WAP_OK, r, "flow lane: context creation failed");
+    ctx->lanes.push_back(h);
+  }
+  for (int q = 0; q < K; ++q) {  // the settings the pairs run with
+    wap_ctx *h = ctx->lanes[q];
+    h->flow_bits = ctx->flow_bits;
+    h->pd_form = ctx->pd_form;
+    h->pd_zchunk = ctx->pd_zchunk;
+    h->pd_plans.clear();  // refilled from the process-wide plans
+    h->pd_plans16.clear();
+    if (ctx->profiling && h->pd_events.empty()) {
+      const int r = wap_set_profiling(h, 1);
+      CHECK(r == WAP_OK, r, "flow lane: " + h->err);
+    }
+    h->profiling = ctx->profiling;
+    h->stats = wap_stats{};
+  }
+  // the lanes start after the work enqueued so far (the volumes the pairs read)
+  ScopedEvents ev(1 + K);
+  CU(ev.create());
+  CU(cudaEventRecord(ev[0], ctx->stream));
+  for (int q = 0; q < K; ++q) CU(cudaStreamWaitEvent(ctx->lanes[q]->stream, ev[0], 0));
+  const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
+  std::atomic<size_t> next{first};
+  std::vector<int> rcs(K, WAP_OK);
+  auto lane = [&](int q) {
+    wap_ctx *h = ctx->lanes[q];
+    try {
+      if (cudaSetDevice(ctx->device) != cudaSuccess) {
+        rcs[q] = fail(h, WAP_ECUDA, "cudaSetDevice failed");
+        return;
+      }
+      for (size_t i; (i = next.fetch_add(1)) < pairs.size();) {
+        const int f = pairs[i];
+        long long total = 0;
+        const int r = flow_multiscale(h, ctx->scan.vol, vol_ptr(ctx, f), vol_ptr(ctx, f + 1), flow_ptr(ctx, f),
+                                      sch->flow_tol, sch->flow_lambda, sch->flow_iters, sch->flow_warps,
+                                      sch->flow_eta, sch->flow_sigma, sch->flow_scales, cut6, flow_ptr(ctx, f),
+                                      &total);
+        if (r != WAP_OK) {
+          rcs[q] = r;
+          return;
+        }
+      }
+    } catch (const std::bad_alloc &) {
+      rcs[q] = WAP_ENOMEM;
+    } catch (...) {
+      rcs[q] = WAP_EHOST;
+    }
+  };
+  std::vector<std::thread> th;
+  int started = 1;
+  try {
+    th.reserve(K - 1);
+    for (; started < K; ++started) th.emplace_back(lane, started);
+  } catch (...) {  // no more threads: fewer lanes (the counter hands them the pairs)
+  }
+  lane(0);
+  for (auto &t : th) t.join();
+  for (int q = 0; q < K; ++q) {
+    if (q < started) {
+      CU(cudaEventRecord(ev[1 + q], ctx->lanes[q]->stream));
+      CU(cudaStreamWaitEvent(ctx->stream, ev[1 + q], 0));
+    }
+    merge_flow_stats(ctx->stats, ctx->lanes[q]->stats);
+  }
+  for (int q = 0; q < K; ++q)
+    if (rcs[q] != WAP_OK) return fail(ctx, rcs[q], "flow lane " + std::to_string(q) + ": " + ctx->lanes[q]->err);
+  return WAP_OK;
+}
+
 // Warp-and-project over the windows of the visited frames in [f0, f1)
 // (WaP_Tomo.cpp:796-822), batched over frames by window slot.
 int wap_pass(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
@@ -1352,6 +1477,7 @@ void wap_destroy(wap_ctx *ctx) {
   cudaStream_t s = ctx->own_stream ? ctx->stream : nullptr;
   for (cudaEvent_t e : ctx->pd_events)
     if (e) cudaEventDestroy(e);
+  for (wap_ctx *h : ctx->lanes) wap_destroy(h);
   g_recycle = idle;  // the stream has drained: the blocks go to the cache
   delete ctx;
   g_recycle = false;
@@ -1429,6 +1555,10 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) try {
   } else if (k == "bp_ray") {
     CHECK(value == 0 || value == 1, WAP_EINVAL, "bp_ray must be 0 or 1");
     ctx->bp_ray = value;
+    return WAP_OK;
+  } else if (k == "flow_lanes") {
+    CHECK(value >= 1 && value <= 8, WAP_EINVAL, "flow_lanes must be 1..8");
+    ctx->flow_lanes = value;
     return WAP_OK;
   } else if (k == "pd_zchunk") {
     CHECK(value >= 0, WAP_EINVAL, "pd_zchunk must be >= 0");
@@ -1792,7 +1922,7 @@ int wap_outer_iteration_frames(wap_ctx *ctx, const wap_schedule *sch, int f0, in
   for (int icp = 1; icp <= sch->n_cp; ++icp) TRY(cp_pass(ctx, sch, f0, f1, icp));
   CU(cudaEventRecord(ev[1], ctx->stream));
   // (2) flow for each adjacent pair (WaP_Tomo.cpp:732-777)
-  for (int f = f0; f < f1 && f + 1 < ctx->F; ++f) TRY(flow_pair(ctx, sch, f));
+  TRY(flow_phase(ctx, sch, f0, f1));
   CU(cudaEventRecord(ev[2], ctx->stream));
   // (3) warp-and-project over each visited frame's window (WaP_Tomo.cpp:796-822)
   TRY(wap_pass(ctx, sch, f0, f1));

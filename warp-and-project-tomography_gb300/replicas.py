@@ -15,11 +15,13 @@ def env_rank():
             int(os.environ.get("LOCAL_RANK", "0")))
 
 
-def frame_order(rank, count, nframes, stride=7):
-    """Frames a rank streams: a rank-specific rotation over the frames that
-    start a flow pair (all but the last), so replicas work on different data."""
-    pairs = max(1, nframes - 1)
-    return [(rank * stride + i) % pairs for i in range(count)]
+def frame_order(rank, count, nframes, stride=7, span=1):
+    """First frames of the steps a rank streams, a step covering `span`
+    consecutive frames each of which starts a flow pair: a rank-specific
+    rotation over the frames f with f + span < nframes, advancing by span, so
+    that replicas work on different data."""
+    starts = max(1, nframes - span)
+    return [(rank * stride + i * span) % starts for i in range(count)]
 
 
 def job_seed(rank, base=0):
