@@ -240,6 +240,33 @@ def test_256_frame_step_bitexact(big, wapmod):
     assert np.array_equal(got_f, want_f), "flow rel L2 %.3g" % rel_l2(got_f, want_f)
 
 
+def test_256_flow_lanes_same_bits(big, wapmod):
+    """The benchmark's two-frame step at 256^3 x 384^2 (frames 0 and 1: their
+    CP and SART work, the two flow pairs they start, their warp-and-project
+    windows; the bounded flow of this module) with the two pairs on two flow
+    lanes at once and one after another: the same volumes and flows of every
+    frame, bit for bit."""
+    ctx = big["ctx"]
+    sched = wapmod.reference_schedule(bp_exact=1, **big["kw"])
+
+    def step(lanes):
+        ctx.set_tuning("flow_lanes", lanes)
+        ctx.level_setup(0)
+        for f in range(F2):
+            ctx.upload_volume(f, big["vols"][f])
+        ctx.outer_iteration_frames(sched, 0, 2)
+        return [ctx.download_volume(f) for f in range(F2)], [ctx.download_flow(f) for f in range(F2)]
+
+    try:
+        step(2)  # a flow shape's first pair runs alone (its plans are tuned undisturbed)
+        one, two = step(1), step(2)
+    finally:
+        ctx.set_tuning("flow_lanes", 2)
+    for f in range(F2):
+        assert np.array_equal(two[0][f], one[0][f]), "volume %d rel L2 %.3g" % (f, rel_l2(two[0][f], one[0][f]))
+        assert np.array_equal(two[1][f], one[1][f]), "flow %d rel L2 %.3g" % (f, rel_l2(two[1][f], one[1][f]))
+
+
 def test_256_precision_form_against_fp64_oracle(big, wapmod):
     """The precision form (flow solver state in FP16 with its fast FP32
     arithmetic, FP32 backprojection) on the same 256^3 frame step: the
