@@ -1273,15 +1273,17 @@ int flow_phase(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
   for (int q = 0; q < K; ++q) CU(cudaStreamWaitEvent(ctx->lanes[q]->stream, ev[0], 0));
   const int cut6[6] = {sch->cut, sch->cut, sch->cut, sch->cut, sch->cut, sch->cut};
   std::atomic<size_t> next{first};
+  std::atomic<bool> failed{false};  // a lane's error: the others take no further pair
   std::vector<int> rcs(K, WAP_OK);
   auto lane = [&](int q) {
     wap_ctx *h = ctx->lanes[q];
     try {
       if (cudaSetDevice(ctx->device) != cudaSuccess) {
         rcs[q] = fail(h, WAP_ECUDA, "cudaSetDevice failed");
+        failed = true;
         return;
       }
-      for (size_t i; (i = next.fetch_add(1)) < pairs.size();) {
+      for (size_t i; !failed && (i = next.fetch_add(1)) < pairs.size();) {
         const int f = pairs[i];
         long long total = 0;
         const int r = flow_multiscale(h, ctx->scan.vol, vol_ptr(ctx, f), vol_ptr(ctx, f + 1), flow_ptr(ctx, f),
@@ -1290,13 +1292,16 @@ int flow_phase(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
                                       &total);
         if (r != WAP_OK) {
           rcs[q] = r;
+          failed = true;
           return;
         }
       }
     } catch (const std::bad_alloc &) {
-      rcs[q] = WAP_ENOMEM;
+      rcs[q] = fail(h, WAP_ENOMEM, "out of memory");  // short: no allocation
+      failed = true;
     } catch (...) {
-      rcs[q] = WAP_EHOST;
+      rcs[q] = fail(h, WAP_EHOST, "host exception");
+      failed = true;
     }
   };
   std::vector<std::thread> th;
