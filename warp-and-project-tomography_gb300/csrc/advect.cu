@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <vector>
 
+#include "f32x2.h"
 #include "wap_internal.h"
 
 namespace wap {
@@ -33,6 +34,28 @@ __device__ __forceinline__ float cubf(float p, float c, float n, float a, float 
     return __fmaf_rn(0.5f * t, __fmaf_rn(__fmaf_rn(C, t, B), t, A), c);
   }
   return c + 0.5f * (t * (-p + n) + t * t * (2 * p - 5 * c + 4 * n - a) + t * t * t * (-p + 3 * c - 3 * n + a));
+}
+
+// cubf on two independent lanes at once (packed FP32, the same operations
+// and order per lane, hence the same bits): two rows of one channel, or one
+// row of two channels.  tt and ttt are t*t and (t*t)*t, as cubf forms them;
+// nz is -0 in both lanes, from a kernel argument (products are fused
+// multiply-adds onto it: f32x2.h).
+template <bool FAST>
+__device__ __forceinline__ f2 cubf2(f2 p, f2 c, f2 n, f2 a, f2 t, f2 tt, f2 ttt, f2 nz) {
+  auto K = [](float k) { return f2_splat(k); };
+  if (FAST) {
+    const f2 A = f2_sub(n, p);
+    const f2 B = f2_fma(K(2.0f), p, f2_fma(K(-5.0f), c, f2_fma(K(4.0f), n, f2_mul(K(-1.0f), a, nz))));
+    const f2 C = f2_fma(K(3.0f), f2_sub(c, n), f2_sub(a, p));
+    return f2_fma(f2_mul(K(0.5f), t, nz), f2_fma(f2_fma(C, t, B), t, A), c);
+  }
+  // -p + n is n - p, and -p + 3c is 3c - p, exactly (IEEE addition commutes)
+  const f2 x1 = f2_mul(t, f2_sub(n, p), nz);
+  const f2 b = f2_sub(f2_add(f2_sub(f2_mul(K(2.0f), p, nz), f2_mul(K(5.0f), c, nz)), f2_mul(K(4.0f), n, nz)), a);
+  const f2 d = f2_add(f2_sub(f2_sub(f2_mul(K(3.0f), c, nz), p), f2_mul(K(3.0f), n, nz)), a);
+  const f2 s = f2_add(f2_add(x1, f2_mul(tt, b, nz)), f2_mul(ttt, d, nz));
+  return f2_add(c, f2_mul(K(0.5f), s, nz));
 }
 
 struct SamplePoint {
@@ -76,7 +99,7 @@ __device__ __forceinline__ SamplePoint locate(const Grid3 &G, float px, float py
 
 // sample_image (advection.h:49-88) of one channel at a located point.
 template <bool FAST>
-__device__ __forceinline__ float sample(const float *__restrict__ img, const Grid3 &G, const SamplePoint &s) {
+__device__ __forceinline__ float sample(const float *__restrict__ img, const Grid3 &G, const SamplePoint &s, f2 nz) {
   const int nx = G.n[0], nxy = G.n[0] * G.n[1];
   auto I = [&](int x, int y, int z) { return __ldg(img + (x + nx * y + nxy * z)); };
   float mn = I(s.ix, s.iy, s.iz), mx = mn;
@@ -90,17 +113,20 @@ __device__ __forceinline__ float sample(const float *__restrict__ img, const Gri
   // One z plane of 16 taps per loop trip (not unrolled): the loads in flight
   // stay at 16 per thread, which keeps the register count low enough for
   // several blocks per SM; the arithmetic and its order are unchanged.
+  // The x cubics of rows (0, 1) and (2, 3) run in pairs.
+  const f2 t = f2_splat(s.dx), tt = f2_mul(t, t, nz), ttt = f2_mul(tt, t, nz);
   float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, p3 = 0.0f;
 #pragma unroll 1
   for (int kz = 0; kz < 4; ++kz) {
     const int z = kz == 0 ? s.zs[0] : kz == 1 ? s.zs[1] : kz == 2 ? s.zs[2] : s.zs[3];
-    float rows[4];
+    f2 rows[2];
 #pragma unroll
-    for (int ky = 0; ky < 4; ++ky) {
-      const int y = s.ys[ky];
-      rows[ky] = cubf<FAST>(I(s.xs[0], y, z), I(s.xs[1], y, z), I(s.xs[2], y, z), I(s.xs[3], y, z), s.dx);
+    for (int h = 0; h < 2; ++h) {
+      const int ya = s.ys[2 * h], yb = s.ys[2 * h + 1];
+      auto tap = [&](int q) { return f2_pack(I(s.xs[q], ya, z), I(s.xs[q], yb, z)); };
+      rows[h] = cubf2<FAST>(tap(0), tap(1), tap(2), tap(3), t, tt, ttt, nz);
     }
-    const float pl = cubf<FAST>(rows[0], rows[1], rows[2], rows[3], s.dy);
+    const float pl = cubf<FAST>(f2_lo(rows[0]), f2_hi(rows[0]), f2_lo(rows[1]), f2_hi(rows[1]), s.dy);
     p0 = kz == 0 ? pl : p0;
     p1 = kz == 1 ? pl : p1;
     p2 = kz == 2 ? pl : p2;
@@ -115,7 +141,7 @@ __device__ __forceinline__ float sample(const float *__restrict__ img, const Gri
 // taps so the index arithmetic is shared and the channels' loads interleave.
 template <bool FAST>
 __device__ __forceinline__ void sample3(const float *__restrict__ vel, size_t nv, const Grid3 &G,
-                                        const SamplePoint &s, float out[3]) {
+                                        const SamplePoint &s, float out[3], f2 nz) {
   const int nx = G.n[0], nxy = G.n[0] * G.n[1];
   auto at = [&](int x, int y, int z) { return x + nx * y + nxy * z; };
   float mn[3], mx[3];
@@ -135,33 +161,39 @@ __device__ __forceinline__ void sample3(const float *__restrict__ vel, size_t nv
       mx[c] = std_max(mx[c], v);
     }
   }
-  float p[3][4];
+  // Channels 0 and 1 run in pairs through all three cubic stages, channel 2
+  // in scalars.
+  const f2 tx = f2_splat(s.dx), ttx = f2_mul(tx, tx, nz), tttx = f2_mul(ttx, tx, nz);
+  const f2 ty = f2_splat(s.dy), tty = f2_mul(ty, ty, nz), ttty = f2_mul(tty, ty, nz);
+  const float *ch0 = vel, *ch1 = vel + nv, *ch2 = vel + 2 * nv;
+  f2 p01[4];
+  float p2[4];
 #pragma unroll 1
   for (int kz = 0; kz < 4; ++kz) {
     const int z = kz == 0 ? s.zs[0] : kz == 1 ? s.zs[1] : kz == 2 ? s.zs[2] : s.zs[3];
-    float rows[3][4];
+    f2 rows01[4];
+    float rows2[4];
 #pragma unroll
     for (int ky = 0; ky < 4; ++ky) {
       const int r = at(0, s.ys[ky], z);
       const int i0 = r + s.xs[0], i1 = r + s.xs[1], i2 = r + s.xs[2], i3 = r + s.xs[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const float *ch = vel + c * nv;
-        rows[c][ky] = cubf<FAST>(__ldg(ch + i0), __ldg(ch + i1), __ldg(ch + i2), __ldg(ch + i3), s.dx);
-      }
+      auto tap = [&](int i) { return f2_pack(__ldg(ch0 + i), __ldg(ch1 + i)); };
+      rows01[ky] = cubf2<FAST>(tap(i0), tap(i1), tap(i2), tap(i3), tx, ttx, tttx, nz);
+      rows2[ky] = cubf<FAST>(__ldg(ch2 + i0), __ldg(ch2 + i1), __ldg(ch2 + i2), __ldg(ch2 + i3), s.dx);
     }
+    const f2 pl01 = cubf2<FAST>(rows01[0], rows01[1], rows01[2], rows01[3], ty, tty, ttty, nz);
+    const float pl2 = cubf<FAST>(rows2[0], rows2[1], rows2[2], rows2[3], s.dy);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const float pl = cubf<FAST>(rows[c][0], rows[c][1], rows[c][2], rows[c][3], s.dy);
-      p[c][0] = kz == 0 ? pl : p[c][0];
-      p[c][1] = kz == 1 ? pl : p[c][1];
-      p[c][2] = kz == 2 ? pl : p[c][2];
-      p[c][3] = kz == 3 ? pl : p[c][3];
+    for (int q = 0; q < 4; ++q) {
+      p01[q] = kz == q ? pl01 : p01[q];
+      p2[q] = kz == q ? pl2 : p2[q];
     }
   }
+  const f2 tz = f2_splat(s.dz), ttz = f2_mul(tz, tz, nz), tttz = f2_mul(ttz, tz, nz);
+  const f2 r01 = cubf2<FAST>(p01[0], p01[1], p01[2], p01[3], tz, ttz, tttz, nz);
+  const float r[3] = {f2_lo(r01), f2_hi(r01), cubf<FAST>(p2[0], p2[1], p2[2], p2[3], s.dz)};
 #pragma unroll
-  for (int c = 0; c < 3; ++c)
-    out[c] = std_max(mn[c], std_min(mx[c], cubf<FAST>(p[c][0], p[c][1], p[c][2], p[c][3], s.dz)));
+  for (int c = 0; c < 3; ++c) out[c] = std_max(mn[c], std_min(mx[c], r[c]));
 }
 
 // 1 in bad[j] when job j's velocity field has a component that is NaN or
@@ -187,7 +219,7 @@ template <bool FAST>
 __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__restrict__ wx,
                                                      const float *__restrict__ wy, const float *__restrict__ wz,
                                                      const AdvectJob *__restrict__ jobs, int nc,
-                                                     const int *__restrict__ bad) {
+                                                     const int *__restrict__ bad, float negzero) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int j = blockIdx.y * blockDim.y + threadIdx.y;
   const int k = blockIdx.z % G.n[2];
@@ -195,6 +227,7 @@ __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__
   const AdvectJob job = jobs[jb];
   if (i >= G.n[0] || j >= G.n[1]) return;
   const bool centre_ok = bad && !bad[jb];
+  const f2 nz = f2_splat(negzero);
   const float *__restrict__ vel = job.vel;
   const float *__restrict__ src = job.src;
   float *__restrict__ out = job.out;
@@ -209,16 +242,16 @@ __global__ void __launch_bounds__(128, 6) advect_kernel(Grid3 G, const float *__
 #pragma unroll
     for (int ch = 0; ch < 3; ++ch) v[ch] = __ldg(vel + ch * nv + c);
   } else {
-    sample3<FAST>(vel, nv, G, s, v);
+    sample3<FAST>(vel, nv, G, s, v, nz);
   }
   const float p2[3] = {p[0] + tdt * v[0], p[1] + tdt * v[1], p[2] + tdt * v[2]};
   s = locate(G, p2[0], p2[1], p2[2]);
-  sample3<FAST>(vel, nv, G, s, v);
+  sample3<FAST>(vel, nv, G, s, v, nz);
   const float p0[3] = {p2[0] - tdt * v[0], p2[1] - tdt * v[1], p2[2] - tdt * v[2]};
   const float q[3] = {p2[0] + (p[0] - p0[0]) * 0.5f, p2[1] + (p[1] - p0[1]) * 0.5f, p2[2] + (p[2] - p0[2]) * 0.5f};
   s = locate(G, q[0], q[1], q[2]);
   const size_t o = i + (size_t)G.n[0] * (j + (size_t)G.n[1] * k);
-  for (int c = 0; c < nc; ++c) out[c * nv + o] = sample<FAST>(src + c * nv, G, s);
+  for (int c = 0; c < nc; ++c) out[c * nv + o] = sample<FAST>(src + c * nv, G, s, nz);
 }
 
 // vol += alpha * adv (double, CImg operator* / operator+=), cut(0, G_Max),
@@ -292,10 +325,10 @@ cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d
     const int *bad = d_flags ? d_flags + j : nullptr;
     if (fast)
       advect_kernel<true><<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1], d_jobs + j,
-                                                  nc, bad);
+                                                  nc, bad, -0.0f);
     else
       advect_kernel<false><<<grid, block, 0, st>>>(G, d_world, d_world + dims[0], d_world + dims[0] + dims[1],
-                                                   d_jobs + j, nc, bad);
+                                                   d_jobs + j, nc, bad, -0.0f);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
