@@ -256,6 +256,15 @@ WAP_API int wap_backproject_ray(wap_ctx *ctx, int proj, const float *d_corr, flo
 WAP_API int wap_advect(wap_ctx *ctx, const int *dims, const float *aabb, const float *d_vel, const float *d_src,
                        int nc, float dt, float *d_out);
 
+/* Self-check of the warp's arithmetic: CImg's cubic evaluated two lanes at a
+ * time in packed FP32 instructions against the scalar evaluation, on n
+ * pseudo-random input pairs drawn from seed (any float bits, subnormals,
+ * signed zeros, dyadic values; fractions mostly in [0, 1)), in the reference
+ * and the precision form's arithmetic.  *h_mismatches = the results whose
+ * bits differ (0 expected; NaN against NaN counts as equal). */
+WAP_API int wap_check_packed_cubic(wap_ctx *ctx, unsigned long long n, unsigned long long seed,
+                                   unsigned long long *h_mismatches);
+
 /* ---- optical flow (device pointers) ------------------------------------- */
 
 /* CImg get_blur(sigma) (Deriche, CImg.h:33276-33285), get_resize(..,5)

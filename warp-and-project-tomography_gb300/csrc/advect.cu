@@ -282,7 +282,65 @@ __global__ void roi_floor_kernel(size_t n, float *__restrict__ vol) {
   vol[i] = mac_max(vol[i] * 1.0f, 0.0f);
 }
 
+// Self-check of the packed cubic: per index, CImg's cubic on two lanes of
+// pseudo-random inputs (any float bits, small dyadic values, tiny and
+// subnormal values, signed zeros; t mostly in [0, 1) as the warp's
+// fractions are) in scalars and in one packed pair, both arithmetics; counts
+// the results whose bits differ (NaN against NaN counts as equal).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {  // splitmix64 finaliser
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ float check_input(unsigned long long h, bool is_t) {
+  const unsigned b = (unsigned)h, kind = (unsigned)(h >> 32) & 7u, sign = (unsigned)(h >> 35) & 1u;
+  if (is_t && kind < 4) return (float)(b >> 8) * 0x1p-24f;  // [0, 1); else any of the kinds below
+  switch (kind) {
+    case 0: return __uint_as_float(b);                                      // any bits
+    case 1: return __uint_as_float((b & 0x007fffffu) | (sign << 31));      // subnormal or zero
+    case 2: return sign ? -0.0f : 0.0f;
+    case 3: return (float)(int)(b & 0xffffu) * 0x1p-12f * (sign ? -1.0f : 1.0f);  // dyadic
+    case 4: return __uint_as_float((b & 0x807fffffu) | (0x00800000u + (b & 0x07000000u)));  // tiny normal
+    default: return __uint_as_float((b & 0x807fffffu) | (((120u + ((b >> 23) & 15u)) & 0xffu) << 23));  // ~1
+  }
+}
+__device__ __forceinline__ bool same_bits(float a, float b) {
+  return __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
+}
+__global__ void cubic_pair_check_kernel(unsigned long long n, unsigned long long seed, float negzero,
+                                        unsigned long long *bad) {
+  const f2 nz = f2_splat(negzero);
+  unsigned long long cnt = 0;
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    float v[2][5];
+#pragma unroll
+    for (int l = 0; l < 2; ++l)
+#pragma unroll
+      for (int q = 0; q < 5; ++q) v[l][q] = check_input(mix64(seed + 10 * i + 5 * l + q), q == 4);
+    const f2 p = f2_pack(v[0][0], v[1][0]), c = f2_pack(v[0][1], v[1][1]), m = f2_pack(v[0][2], v[1][2]),
+             a = f2_pack(v[0][3], v[1][3]);
+    // the pair's t differs per lane here (in the warp both lanes share one t)
+    const f2 t = f2_pack(v[0][4], v[1][4]), tt = f2_mul(t, t, nz), ttt = f2_mul(tt, t, nz);
+    const f2 r = cubf2<false>(p, c, m, a, t, tt, ttt, nz), rf = cubf2<true>(p, c, m, a, t, tt, ttt, nz);
+#pragma unroll
+    for (int l = 0; l < 2; ++l) {
+      const float e = cubf<false>(v[l][0], v[l][1], v[l][2], v[l][3], v[l][4]);
+      const float ef = cubf<true>(v[l][0], v[l][1], v[l][2], v[l][3], v[l][4]);
+      cnt += !same_bits(l ? f2_hi(r) : f2_lo(r), e);
+      cnt += !same_bits(l ? f2_hi(rf) : f2_lo(rf), ef);
+    }
+  }
+  if (cnt) atomicAdd(bad, cnt);
+}
+
 }  // namespace
+
+cudaError_t launch_cubic_pair_check(unsigned long long n, unsigned long long seed, unsigned long long *d_bad,
+                                    cudaStream_t st) {
+  cubic_pair_check_kernel<<<152 * 8, 256, 0, st>>>(n, seed, -0.0f, d_bad);
+  return cudaGetLastError();
+}
 
 void world_table(const int dims[3], const float aabb[6], float *h) {
   int off = 0;

@@ -1845,6 +1845,19 @@ int wap_resize(wap_ctx *ctx, const int *dims, int nc, const float *d_src, const 
   return do_resize(ctx, dims, nc, d_src, odims, d_out);
 } WAP_CATCH
 
+int wap_check_packed_cubic(wap_ctx *ctx, unsigned long long n, unsigned long long seed,
+                           unsigned long long *h_mismatches) try {
+  CHECK(ctx && h_mismatches, WAP_EINVAL, "null argument");
+  CU(cudaSetDevice(ctx->device));
+  DevMem bad;
+  CU(bad.ensure(sizeof(unsigned long long)));
+  CU(cudaMemsetAsync(bad.p, 0, sizeof(unsigned long long), ctx->stream));
+  KL(launch_cubic_pair_check(n, seed, bad.as<unsigned long long>(), ctx->stream));
+  CU(cudaMemcpyAsync(h_mismatches, bad.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return WAP_OK;
+} WAP_CATCH
+
 int wap_flow_level(wap_ctx *ctx, const int *dims, const float *d_I1, const float *d_I2, float *d_V, float *d_Y1,
                    float *d_Y2, float *d_Y3, float *d_Y4, float tol, float lambda, int max_iters, int nwarps,
                    const float *aabb, const int *roi6, int *h_iters) try {

@@ -187,6 +187,11 @@ cudaError_t launch_advect(const int dims[3], const float aabb[6], const float *d
 cudaError_t launch_wap_accumulate(size_t n, float *vol, const float *adv, double alpha, float gmax, cudaStream_t st,
                                   bool floor = true);
 cudaError_t launch_roi_floor(size_t n, float *vol, cudaStream_t st);
+// Adds to *d_bad the number of n pseudo-random inputs (from seed) on which the
+// warp's packed-pair cubic and its scalar cubic differ in bits, in both the
+// reference and the fast arithmetic.
+cudaError_t launch_cubic_pair_check(unsigned long long n, unsigned long long seed, unsigned long long *d_bad,
+                                    cudaStream_t st);
 struct AccJob {
   float *vol;
   const float *adv;

@@ -134,6 +134,7 @@ SIGNATURES = {
     "wap_advect": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_int, _c_float, _vp]),
     "wap_blur": (_c_int, [_vp, _vp, _c_int, _c_float, _vp, _vp]),
     "wap_resize": (_c_int, [_vp, _vp, _c_int, _vp, _vp, _vp]),
+    "wap_check_packed_cubic": (_c_int, [_vp, ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)]),
     "wap_flow_level": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_float, _c_float, _c_int, _c_int,
                                 _vp, _vp, _vp]),
     "wap_flow_multiscale": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_float, _c_float, _c_int, _c_int, _c_float,
@@ -399,6 +400,13 @@ class Context:
     def resize(self, dims, nc, d_src, odims, d_out):
         d, o = _ints(dims), _ints(odims)
         self.call("wap_resize", d.ctypes.data, nc, ptr(d_src), o.ctypes.data, ptr(d_out))
+
+    def check_packed_cubic(self, n, seed=0):
+        """Bit mismatches between the warp's packed-pair cubic and the scalar
+        one on n pseudo-random input pairs (0 expected)."""
+        bad = ctypes.c_ulonglong(0)
+        self.call("wap_check_packed_cubic", n, seed, ctypes.byref(bad))
+        return bad.value
 
     def flow_level(self, dims, dI1, dI2, dV, dY1, dY2, dY3, dY4, tol, lam, iters, nwarps, aabb, roi6):
         d, a, r = _ints(dims), _floats(aabb), _ints(roi6)
