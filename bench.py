@@ -95,8 +95,9 @@ def parse():
     ap.add_argument("--frames-per-step", type=int, default=2,
                     help="consecutive frames a step covers: their CP and SART work, their flow pairs (which run "
                          "concurrently on the library's flow lanes) and their warp-and-project windows")
-    ap.add_argument("--flow-lanes", type=int, default=2,
-                    help="flow pairs the library runs concurrently (its flow_lanes tuning key)")
+    ap.add_argument("--flow-lanes", type=int, default=0,
+                    help="flow pairs the library runs concurrently (its flow_lanes tuning key; 0: the library's "
+                         "automatic choice, 2 lanes at 256^3)")
     ap.add_argument("--full-outer", action="store_true",
                     help="also time one whole outer iteration (all frames in pass order; minutes at 256^3)")
     ap.add_argument("--save-outer-counts", default="",

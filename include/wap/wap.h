@@ -162,10 +162,11 @@ WAP_API int wap_set_observer(wap_ctx *ctx, wap_observer_fn fn, void *user);
  * TMA-fed fused kernel (grids with nx % 4 == 0, else 2); "pd_zchunk": z
  * planes per block, 0 = autotuned / default; "fp_bricks": 1 (default) = the
  * forward projector reads a 4x4x4 brick-layout copy of each volume, 0 = the
- * linear volume.  "flow_lanes": 2 (default) = an outer iteration's flow
- * pairs run concurrently on two lanes (helper contexts with their own
- * streams and workspaces; each pair's flow is the one it gets alone), 1 =
- * one pair after another, up to 8.  "bp_ray": 0 (default) = SART backprojects voxel-driven
+ * linear volume.  "flow_lanes": an outer iteration's flow pairs run
+ * concurrently on this many lanes (helper contexts with their own streams
+ * and workspaces; each pair's flow is the one it gets alone), 1 = one pair
+ * after another, up to 8; 0 (default) = automatic: 4 lanes for volumes of at
+ * most 128^3 voxels, whose flow levels are latency-bound, 2 above.  "bp_ray": 0 (default) = SART backprojects voxel-driven
  * with the reference's bicubic weights; 1 = SART backprojects with the
  * matched ray-driven splat (the ray caster's back-projection mode,
  * SingleScalarVolume.core.h:85-96,149-199, which the reference's

@@ -261,7 +261,7 @@ def test_256_flow_lanes_same_bits(big, wapmod):
         step(2)  # a flow shape's first pair runs alone (its plans are tuned undisturbed)
         one, two = step(1), step(2)
     finally:
-        ctx.set_tuning("flow_lanes", 2)
+        ctx.set_tuning("flow_lanes", 0)
     for f in range(F2):
         assert np.array_equal(two[0][f], one[0][f]), "volume %d rel L2 %.3g" % (f, rel_l2(two[0][f], one[0][f]))
         assert np.array_equal(two[1][f], one[1][f]), "flow %d rel L2 %.3g" % (f, rel_l2(two[1][f], one[1][f]))

@@ -459,9 +459,10 @@ def test_outer_iteration_steps_equal_the_whole(setup, wapmod):
 
 def test_flow_lanes_give_the_same_outer_iteration(wapmod, orc, torch_cuda):
     """An outer iteration's flow pairs run concurrently on helper lanes
-    (flow_lanes 2 and 3) or one after another (1): the same volumes, flows and
-    primal-dual iteration counts bit for bit, on a 6-frame scan (5 pairs), with
-    the 0.008 tolerance so that levels stop early."""
+    (flow_lanes 2, 3, 4 and the automatic choice, 4 at this size) or one
+    after another (1): the same volumes, flows and primal-dual iteration
+    counts bit for bit, on a 6-frame scan (5 pairs), with the 0.008 tolerance
+    so that levels stop early."""
     import oracle as O
     n, d, nproj = 32, 48, 24
     vol = P.ellipsoids(n, seed=21)
@@ -474,14 +475,14 @@ def test_flow_lanes_give_the_same_outer_iteration(wapmod, orc, torch_cuda):
         sched = wapmod.reference_schedule(n_cp=2, nb_sart=2, wp_frames=6, flow_iters=120, flow_scales=2,
                                           flow_tol=0.008, flow_warps=2)
         got = {}
-        for lanes in (1, 2, 3):
+        for lanes in (1, 2, 3, 4, 0):
             ctx.set_tuning("flow_lanes", lanes)
             F = ctx.level_setup(0)
             assert F == 6
             st = ctx.outer_iteration(sched)
             got[lanes] = ([ctx.download_volume(f) for f in range(F)], [ctx.download_flow(f) for f in range(F)],
                           int(st.flow_pd_iterations))
-        for lanes in (2, 3):
+        for lanes in (2, 3, 4, 0):
             assert got[lanes][2] == got[1][2]
             for f in range(6):
                 assert np.array_equal(got[lanes][0][f], got[1][0][f]), (lanes, f)

@@ -248,7 +248,10 @@ struct wap_ctx {
   int pd_form = 0;    // 0: autotuned, 1: fused kernel, 2: primal + dual kernels
   int pd_zchunk = 0;  // 0: autotuned / default
   int flow_bits = 32; // 16: the flow solver's y, v, u stored in FP16 (the precision form)
-  int flow_lanes = 2; // flow pairs of an outer iteration run concurrently on this many lanes (1: in turn)
+  // flow pairs of an outer iteration run concurrently on this many lanes (1: in
+  // turn; 0: automatic, kAutoLanesSmall for a flow grid of at most
+  // kAutoLanesSmallVoxels, whose levels are latency-bound, else 2)
+  int flow_lanes = 0;
   std::vector<wap_ctx *> lanes;  // the lanes: helper compute contexts, each with its own stream and workspaces
   std::set<std::tuple<int, int, int, int, int, int>> lanes_tuned;  // flow shapes whose plans are tuned
   std::map<std::tuple<int, int, int>, std::pair<int, int>> pd_plans;  // grid -> (form, zchunk)
@@ -1230,6 +1233,13 @@ void merge_flow_stats(wap_stats &d, const wap_stats &s) {
 // The pairs run in turn when an observer is set (its events come in pair
 // order), when one pair is due, and the first time a flow shape is seen, so
 // that the autotuner times its candidates undisturbed.
+// Automatic lane count: measured outer iterations (16 frames, fixed 3000
+// primal-dual iterations per warp and level) with 2 / 4 lanes: 64^3 2.01 /
+// 1.57 s, 96^3 4.60 / 4.46 s, 128^3 8.45 / 8.23 s; at 256^3 two lanes, whose
+// finest levels stream from HBM, are as fast as three.
+constexpr size_t kAutoLanesSmallVoxels = (size_t)128 * 128 * 128;
+constexpr int kAutoLanesSmall = 4;
+
 int flow_phase(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
   std::vector<int> pairs;
   for (int f = f0; f < f1 && f + 1 < ctx->F; ++f) pairs.push_back(f);
@@ -1241,7 +1251,9 @@ int flow_phase(wap_ctx *ctx, const wap_schedule *sch, int f0, int f1) {
     ctx->lanes_tuned.insert(shape);
     first = 1;
   }
-  const int K = std::min<int>(ctx->flow_lanes, (int)(pairs.size() - first));
+  const size_t nv = (size_t)ctx->scan.vol[0] * ctx->scan.vol[1] * ctx->scan.vol[2];
+  const int lanes = ctx->flow_lanes > 0 ? ctx->flow_lanes : nv <= kAutoLanesSmallVoxels ? kAutoLanesSmall : 2;
+  const int K = std::min<int>(lanes, (int)(pairs.size() - first));
   if (K <= 1 || ctx->observer) {
     for (size_t i = first; i < pairs.size(); ++i) TRY(flow_pair(ctx, sch, pairs[i]));
     return WAP_OK;
@@ -1562,7 +1574,7 @@ int wap_set_tuning(wap_ctx *ctx, const char *key, int value) try {
     ctx->bp_ray = value;
     return WAP_OK;
   } else if (k == "flow_lanes") {
-    CHECK(value >= 1 && value <= 8, WAP_EINVAL, "flow_lanes must be 1..8");
+    CHECK(value >= 0 && value <= 8, WAP_EINVAL, "flow_lanes must be 0 (automatic) .. 8");
     ctx->flow_lanes = value;
     return WAP_OK;
   } else if (k == "pd_zchunk") {
